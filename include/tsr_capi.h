@@ -1,0 +1,165 @@
+/*
+ * tsr_capi.h -- C-ABI of the GB300 two-scale Richards hot path.
+ *
+ * Plain pointers and sizes only.  Every call returns a status code (TSR_OK =
+ * 0) and none calls exit(); tsr_last_error_message() describes the last
+ * failure of the calling thread.  One process drives one GPU; a context owns
+ * the device copy of the mesh geometry and every work buffer it needs, so the
+ * per-call paths allocate nothing.
+ *
+ * Each entry point names the reference interface it replaces (paths inside
+ * the TwoScaleRich source tree).  The C++ drop-ins with the reference's exact
+ * signatures (Gfunc_gpu, exprem_gpu) are in tsr_dropin.hpp and are thin
+ * wrappers over these functions.
+ */
+#ifndef TSR_CAPI_H
+#define TSR_CAPI_H
+
+#include "tsr_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define TSR_OK             0
+#define TSR_ERR_CUDA       1   /* a CUDA runtime call failed */
+#define TSR_ERR_NAN        2   /* non-finite value met in a device reduction */
+#define TSR_ERR_BOUNDS     3   /* an index of the mesh data is out of range */
+#define TSR_ERR_TIMEOUT    4   /* a bounded device wait ran out */
+#define TSR_ERR_ARG        5   /* invalid argument or unsupported mesh */
+#define TSR_ERR_ALLOC      6   /* allocation failed */
+#define TSR_ERR_SINGULAR   7   /* singular Pade denominator in phipade */
+#define TSR_ERR_MINSTEP    8   /* step size fell below MinStep */
+#define TSR_ERR_MAXSTEPS   9   /* MaxNumSteps reached */
+#define TSR_ERR_GFUNC     10   /* G evaluation reported a failure flag */
+#define TSR_ERR_IO        11   /* file missing or malformed */
+
+typedef struct tsr_ctx tsr_ctx;
+
+int         tsr_version(void);
+const char* tsr_last_error_message(void);
+
+/* ---- host-side set-up (reference layer L0/L1, kept on the host) ------- */
+
+/* Replaces macro_mesh_properties(const char*, macro_mesh_struct&, int*)
+ * (src/macro_mesh_properties.cpp:15; prototype include/main.h:23).  Reads the
+ * reference's macro mesh text format.  macro_bc[j] is the BC type of boundary
+ * tag -(j+1), j = 0..4.  Returns TSR_ERR_IO where the reference returns 1. */
+int tsr_macro_mesh_properties(const char* mesh_file, macro_mesh_struct* mesh,
+                              const int* macro_bc);
+
+/* Same geometry from in-memory arrays: xy[2*n_nodes] (x block then y
+ * block), elems[nv*n_elems] 0-based and element-major (vertex v of element k
+ * at k*nv+v), bedges[3*n_bedges] = (node a, node b, tag) 0-based nodes. */
+int tsr_macro_mesh_build(int nv, int n_nodes, const double* xy, int n_elems,
+                         const int* elems, int n_bedges, const int* bedges,
+                         const int* macro_bc, macro_mesh_struct* mesh);
+
+/* Replaces micro_mesh_properties(const char*, micro_mesh_struct&)
+ * (src/micro_mesh_properties.cpp:15; include/main.h:25). */
+int tsr_micro_mesh_properties(const char* mesh_file, micro_mesh_struct* mesh);
+
+int tsr_micro_mesh_build(double cell_width, double cell_height, int nv,
+                         int n_nodes, const double* xy, int n_elems,
+                         const int* elems, int n_bedges, const int* bedges,
+                         micro_mesh_struct* mesh);
+
+/* Replaces read_effective_conductivity(const char*, Keff_struct&)
+ * (src/read_effective_conductivity.cpp:15; include/main.h:26). */
+int tsr_read_effective_conductivity(const char* Keff_file, Keff_struct* keff);
+
+/* Replaces set_exprem_options(exprem_options_struct&)
+ * (src/set_exprem_options.cpp:14; include/main.h:28). */
+int tsr_set_exprem_options(exprem_options_struct* options);
+
+void tsr_macro_mesh_free(macro_mesh_struct* mesh);
+void tsr_micro_mesh_free(micro_mesh_struct* mesh);
+void tsr_keff_free(Keff_struct* keff);
+
+/* Replaces phipade(double*, double*, double, int, int)
+ * (src/phipade.cpp:15; include/exprem.h:28): phi_1(alpha*H(1:m,1:m)) by the
+ * (6,6) Pade approximant with scaling and squaring, FP64 on the host.  H has
+ * leading dimension MaxKrylov+1, phiH leading dimension MaxKrylov (column
+ * major).  Returns TSR_ERR_SINGULAR where the reference calls exit(). */
+int tsr_phipade(double* phiH, const double* H, double alpha, int m,
+                int MaxKrylov);
+
+/* ---- device context ---------------------------------------------------- */
+
+/* Uploads the geometry of user_data once (arrays are treated as immutable
+ * afterwards, as in the reference, include/user_data.h:1-11).  stream may be
+ * NULL (the context creates its own non-blocking stream).  max_krylov sizes
+ * the resident Krylov basis (N x (max_krylov+1) doubles); 0 = no basis (G
+ * and Jv only).  Returns NULL on failure. */
+tsr_ctx* tsr_init(const user_data_struct* user_data, const tsr_model_ext* ext,
+                  void* stream, int max_krylov);
+void     tsr_free(tsr_ctx* ctx);
+void*    tsr_stream(tsr_ctx* ctx);
+int      tsr_num_unknowns(tsr_ctx* ctx);
+
+/* g = G(u), the two-scale right-hand side.  Replaces Gfunc_serial /
+ * Gfunc_parallel (int Gfunc(double* g, double* u, user_data_struct),
+ * include/main.h:21-22, selected at src/main.cpp:198-213).  Host pointers;
+ * copies in, computes on the GPU, copies out, synchronizes. */
+int tsr_g_eval(tsr_ctx* ctx, const double* u, double* g);
+
+/* Same on device pointers, asynchronous on the context stream. */
+int tsr_g_eval_device(tsr_ctx* ctx, const double* d_u, double* d_g);
+
+/* Finite-difference Jacobian-vector product of the EXPREM Arnoldi loop:
+ * w = (G(u + eps v) - g0) * (1/eps).  Host pointers. */
+int tsr_jv(tsr_ctx* ctx, const double* u, const double* g0, const double* v,
+           double eps, double* w);
+int tsr_jv_device(tsr_ctx* ctx, const double* d_u, const double* d_g0,
+                  const double* d_v, double eps, double* d_w);
+
+/* Total water content of state u [m^3 per m of depth]:
+ * sum_i eps_A theta_A(H_i) CV_i + sum_k (|element k| / |Y|) sum_l theta_B(h_l) A_l. */
+int tsr_water_content(tsr_ctx* ctx, const double* u, double* water);
+
+/* Deterministic FP64 dot product in the library's fixed reduction order
+ * (the order every Arnoldi reduction uses).  Host pointers; for tests. */
+int tsr_dot(tsr_ctx* ctx, const double* x, const double* y, int n, double* out);
+
+/* ---- EXPREM (exponential Rosenbrock-Euler, Krylov) --------------------- */
+
+/* One accepted step, as the reference's exprem(...) (include/main.h:29-32,
+ * called once per iteration at src/main.cpp:316): advances *t and u0 (host,
+ * N doubles) by one accepted step no larger than tend - *t, writes every
+ * tspan time it crosses into tspan_solns (row k at k*N, tspan[0] = count),
+ * and updates stats.  The solver state (u, g(u), the Krylov basis) lives on
+ * the GPU; u0 is copied in and out on every call.  The first call (t == 0)
+ * initialises stats, as the reference leaves them uninitialised
+ * (src/main.cpp:257).  Returns TSR_OK, or an error code where the reference
+ * returns -1. */
+int tsr_exprem_step(tsr_ctx* ctx, double* t, double tend, const double* tspan,
+                    double* tspan_solns, double* u0,
+                    const exprem_options_struct* options,
+                    exprem_stats_struct* stats);
+
+/* Device-resident stepping for callers that keep u on the GPU: load the
+ * state once, advance, read back when needed. */
+int tsr_exprem_load(tsr_ctx* ctx, const double* u_host, double t);
+int tsr_exprem_advance(tsr_ctx* ctx, double tend, const double* tspan,
+                       double* tspan_solns, const exprem_options_struct* options,
+                       exprem_stats_struct* stats, double* t_out);
+int tsr_exprem_store(tsr_ctx* ctx, double* u_host);
+
+/* C entry with the data of the C++ drop-in Gfunc_gpu (tsr_dropin.hpp):
+ * g = G(u) for the context registered for user_data (created on first use,
+ * keyed by the address of its macro element array). */
+int tsr_gfunc_gpu(double* g, double* u, const user_data_struct* user_data);
+
+/* Registers the model extension used by contexts that tsr_gfunc_gpu and
+ * exprem_gpu create implicitly (call before their first use). */
+int tsr_set_default_ext(const tsr_model_ext* ext, int max_krylov);
+
+/* Releases every implicitly created context. */
+void tsr_release_all(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TSR_CAPI_H */

@@ -1,0 +1,867 @@
+// tsr_ctx.cu -- device context, C-ABI entry points and the EXPREM driver.
+//
+// A context uploads the mesh once (the reference treats the user_data arrays
+// as immutable after set-up, include/user_data.h) and owns every device
+// buffer the hot path needs, so G, Jv and EXPREM steps allocate nothing.
+// The EXPREM step runs its vector work on the GPU (u, G(u), the Krylov basis
+// V and all N-length temporaries stay in HBM) and crosses to the host only
+// for the (m+1) x m Hessenberg column, a few scalars and phi_1(dt H_m).
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/tsr_capi.h"
+#include "tsr_device.h"
+#include "tsr_internal.h"
+#include "tsr_math.h"
+
+using namespace tsr;
+
+namespace {
+
+constexpr double kKrylovTol = 0.1;   // Krylov error accepted as a fraction of the step tolerance
+constexpr int kMaxKrylovCap = 512;
+
+// device scalar slots after the Hessenberg block
+enum { S_HSQ = 0, S_SV, S_ERR, S_DOT, S_BETA2, S_NU2, S_WATER, S_IH, S_COUNT = 16 };
+
+}  // namespace
+
+struct tsr_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    Problem P{};
+    long long N = 0;
+    int Mn = 0, Ne = 0;
+    std::vector<void*> allocs;
+    // work buffers
+    double *d_u = nullptr, *d_g0 = nullptr, *d_g1 = nullptr, *d_w = nullptr, *d_unew = nullptr;
+    double *d_winv = nullptr, *d_x = nullptr, *d_y = nullptr, *d_z = nullptr, *d_V = nullptr;
+    double *d_terms = nullptr, *d_scal = nullptr, *d_coef = nullptr;
+    double* h_scal = nullptr;   // pinned mirror of d_scal
+    double* h_coef = nullptr;   // pinned coefficients upload
+    int* h_flag = nullptr;      // pinned
+    RedWork rw{};
+    int maxk = 0;
+    int ldH = 0;
+    // EXPREM state
+    bool state_loaded = false;
+    double t_state = 0.0;
+    bool g0_valid = false;
+    const double* last_u0 = nullptr;
+    double last_t = -1.0;
+    std::vector<double> Hm, phi;
+};
+
+namespace {
+
+const char* cuda_msg(cudaError_t e) { return cudaGetErrorString(e); }
+
+#define CK(call)                                                                 \
+    do {                                                                         \
+        cudaError_t e_ = (call);                                                 \
+        if (e_ != cudaSuccess) {                                                 \
+            set_error(std::string(#call) + ": " + cuda_msg(e_));                 \
+            return TSR_ERR_CUDA;                                                 \
+        }                                                                        \
+    } while (0)
+
+template <typename T>
+int upload(tsr_ctx* c, const T* host, size_t n, const T** out)
+{
+    void* p = nullptr;
+    size_t bytes = sizeof(T) * (n > 0 ? n : 1);
+    CK(cudaMalloc(&p, bytes));
+    c->allocs.push_back(p);
+    if (n > 0 && host) CK(cudaMemcpy(p, host, sizeof(T) * n, cudaMemcpyHostToDevice));
+    *out = static_cast<const T*>(p);
+    return TSR_OK;
+}
+
+int dev_alloc(tsr_ctx* c, size_t bytes, void** out)
+{
+    void* p = nullptr;
+    CK(cudaMalloc(&p, bytes > 0 ? bytes : 8));
+    c->allocs.push_back(p);
+    *out = p;
+    return TSR_OK;
+}
+
+VGPar make_vg(const soil_struct& s)
+{
+    VGPar p;
+    p.Ks = s.Ksat;
+    p.thr = s.thetar;
+    p.ths = s.thetas;
+    p.alpha = s.alpha;
+    p.n = s.n;
+    p.m = s.m;
+    p.dth = s.thetas - s.thetar;
+    p.coefC = (p.dth * s.m) * s.n;
+    p.mh = -0.5 * s.m;
+    return p;
+}
+
+// Per-node lists of (item, sign) in the order the element loop of the
+// CVFE assembly scatters them.
+struct Csr {
+    std::vector<int> ptr, ent;
+};
+
+Csr group_events(int n_nodes, const std::vector<int>& node, const std::vector<int>& code)
+{
+    Csr c;
+    c.ptr.assign((size_t)n_nodes + 1, 0);
+    for (int v : node) c.ptr[(size_t)v + 1]++;
+    for (int i = 0; i < n_nodes; ++i) c.ptr[(size_t)i + 1] += c.ptr[i];
+    std::vector<int> fill(c.ptr.begin(), c.ptr.end() - 1);
+    c.ent.assign(node.size(), 0);
+    for (size_t e = 0; e < node.size(); ++e) c.ent[(size_t)fill[node[e]]++] = code[e];
+    return c;
+}
+
+int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* ext)
+{
+    const macro_mesh_struct& M = ud.macro_mesh;
+    const micro_mesh_struct& m = ud.micro_mesh;
+    if (M.no_verts != 3 && M.no_verts != 4) {
+        set_error("macro mesh must have 3 or 4 vertices per element");
+        return TSR_ERR_ARG;
+    }
+    if (m.no_verts != 3) {
+        set_error("micro mesh must be triangular");
+        return TSR_ERR_ARG;
+    }
+    if (ud.model_type < 1 || ud.model_type > 3) {
+        set_error("model_type must be 1, 2 or 3");
+        return TSR_ERR_ARG;
+    }
+    const int nv = M.no_verts, Ne = M.no_elements, Mn = M.no_nodes;
+    const int mn = m.no_nodes, mNe = m.no_elements;
+    const long long N = (long long)Mn + (long long)Ne * mn;
+    if (N > 0x7fffffffLL || (long long)Ne * 32 > 0x7fffffffLL) {
+        set_error("problem too large for 32-bit indices");
+        return TSR_ERR_ARG;
+    }
+    if (ud.N != 0 && ud.N != (int)N) {
+        set_error("user_data.N does not match the meshes");
+        return TSR_ERR_ARG;
+    }
+    for (long long i = 0; i < (long long)nv * Ne; ++i)
+        if (M.elements[i] < 0 || M.elements[i] >= Mn) {
+            set_error("macro element index out of range");
+            return TSR_ERR_BOUNDS;
+        }
+    for (long long i = 0; i < 3LL * mNe; ++i)
+        if (m.elements[i] < 0 || m.elements[i] >= mn) {
+            set_error("micro element index out of range");
+            return TSR_ERR_BOUNDS;
+        }
+    c->N = N;
+    c->Mn = Mn;
+    c->Ne = Ne;
+    Problem& P = c->P;
+    P.N = N;
+    MacroDev& D = P.M;
+    D.Mn = Mn;
+    D.Ne = Ne;
+    D.nv = nv;
+    D.model_type = ud.model_type;
+    int rc;
+    const size_t nvNe = (size_t)nv * Ne;
+    if ((rc = upload(c, M.elements, nvNe, &D.elements))) return rc;
+    if ((rc = upload(c, M.shape_funcs, (size_t)nv * nvNe, &D.sf))) return rc;
+    if ((rc = upload(c, M.normals, 2 * nvNe, &D.normals))) return rc;
+    if ((rc = upload(c, M.midx, nvNe, &D.midx))) return rc;
+    if ((rc = upload(c, M.midy, nvNe, &D.midy))) return rc;
+    if ((rc = upload(c, M.boundary_condition_edges, nvNe, &D.bce))) return rc;
+    if ((rc = upload(c, M.boundary_edge_lens, 2 * nvNe, &D.blen))) return rc;
+    if ((rc = upload(c, M.boundary_edge_midpts, 4 * nvNe, &D.bmid))) return rc;
+    if ((rc = upload(c, M.boundary_edge_normals, 4 * nvNe, &D.bnrm))) return rc;
+    if ((rc = upload(c, M.SCV_area, nvNe, &D.scv))) return rc;
+    if ((rc = upload(c, M.CV_area, (size_t)Mn, &D.cv))) return rc;
+    if ((rc = upload(c, M.centroid_elements, 2 * (size_t)Ne, &D.cent))) return rc;
+    // Dirichlet nodes: end nodes of type-5 edges
+    std::vector<unsigned char> dir((size_t)Mn, 0);
+    for (int k = 0; k < Ne; ++k)
+        for (int j = 0; j < nv; ++j)
+            if (M.boundary_condition_edges[(size_t)j * Ne + k] == TSR_BC_DIRICHLET) {
+                dir[M.elements[(size_t)j * Ne + k]] = 1;
+                dir[M.elements[(size_t)((j + 1) % nv) * Ne + k]] = 1;
+            }
+    if ((rc = upload(c, dir.data(), dir.size(), &D.dirichlet))) return rc;
+    // macro scatter lists, in the order of the element loop: faces, boundary
+    // halves, exchange (slot 16k + s, sign bit 0 = add)
+    {
+        std::vector<int> node, code;
+        node.reserve((size_t)Ne * 16);
+        code.reserve((size_t)Ne * 16);
+        for (int k = 0; k < Ne; ++k) {
+            int v[4];
+            for (int j = 0; j < nv; ++j) v[j] = M.elements[(size_t)j * Ne + k];
+            for (int j = 0; j < nv; ++j) {
+                node.push_back(v[j]);
+                code.push_back((16 * k + j) << 1);
+                node.push_back(v[(j + 1) % nv]);
+                code.push_back(((16 * k + j) << 1) | 1);
+            }
+            for (int j = 0; j < nv; ++j) {
+                int bc = M.boundary_condition_edges[(size_t)j * Ne + k];
+                if (bc != TSR_BC_FLUX && bc != TSR_BC_DHDX0 && bc != TSR_BC_DHDY0) continue;
+                for (int sh = 0; sh < 2; ++sh) {
+                    node.push_back(v[(j + sh) % nv]);
+                    code.push_back((16 * k + nv + 2 * j + sh) << 1);
+                }
+            }
+            if (ud.model_type == 3)
+                for (int j = 0; j < nv; ++j) {
+                    node.push_back(v[j]);
+                    code.push_back(((16 * k + 3 * nv + j) << 1) | 1);
+                }
+        }
+        Csr csr = group_events(Mn, node, code);
+        if ((rc = upload(c, csr.ptr.data(), csr.ptr.size(), &D.csr_ptr))) return rc;
+        if ((rc = upload(c, csr.ent.data(), csr.ent.size(), &D.csr_ent))) return rc;
+    }
+    const Keff_struct& K = ud.effective_conductivity;
+    if (K.no_hvalues < 1 || !K.Keff_values) {
+        set_error("empty effective conductivity table");
+        return TSR_ERR_ARG;
+    }
+    D.nk = K.no_hvalues;
+    if ((rc = upload(c, K.Keff_values, 4 * (size_t)K.no_hvalues, &D.keff))) return rc;
+    D.keff_first = K.logh_first;
+    D.keff_inv_logr = 1.0 / K.logr;
+    D.epsA = K.epsilonA;
+    D.inv_Y = 1.0 / m.cell_area;
+    D.Ss = (ext && ext->specific_storage > 0.0) ? ext->specific_storage : 1e-6;
+    D.bflux = ud.boundary_flux;
+    P.pA = make_vg(ud.soilA);
+    P.pB = make_vg(ud.soilB);
+    P.kface = ext ? ext->kface_mode : 0;
+    P.cell_scale = nullptr;
+    if (ext && ext->cell_scale) {
+        if ((rc = upload(c, ext->cell_scale, (size_t)Ne, &P.cell_scale))) return rc;
+    }
+    // micro template
+    MicroTpl& T = P.m;
+    T.mn = mn;
+    T.mNe = mNe;
+    {
+        std::vector<int> ev(3 * (size_t)mNe);
+        std::vector<double> eg(12 * (size_t)mNe);
+        std::vector<int> node, code, ebf((size_t)mNe, 0), ebc((size_t)mNe, 0), bv;
+        std::vector<double> bn;
+        for (int e = 0; e < mNe; ++e) {
+            int v[3];
+            for (int j = 0; j < 3; ++j) v[j] = ev[3 * (size_t)e + j] = m.elements[(size_t)j * mNe + e];
+            for (int r = 0; r < 6; ++r) eg[12 * (size_t)e + r] = m.shape_funcs[(size_t)r * mNe + e];
+            for (int j = 0; j < 3; ++j)
+                for (int d = 0; d < 2; ++d)
+                    eg[12 * (size_t)e + 6 + 2 * j + d] = m.normals[(size_t)(2 * j + d) * mNe + e];
+            for (int j = 0; j < 3; ++j) {
+                node.push_back(v[j]);
+                code.push_back((3 * e + j) << 1);
+                node.push_back(v[(j + 1) % 3]);
+                code.push_back(((3 * e + j) << 1) | 1);
+            }
+            ebf[e] = (int)bv.size();
+            for (int j = 0; j < 3; ++j) {
+                if (m.boundary_edges[(size_t)j * mNe + e] != 1) continue;
+                for (int sh = 0; sh < 2; ++sh) {
+                    bv.push_back(v[(j + sh) % 3]);
+                    bn.push_back(m.boundary_edge_normals[(size_t)(4 * j + 2 * sh) * mNe + e]);
+                    bn.push_back(m.boundary_edge_normals[(size_t)(4 * j + 2 * sh + 1) * mNe + e]);
+                }
+            }
+            ebc[e] = (int)bv.size() - ebf[e];
+        }
+        T.nb = (int)bv.size();
+        Csr csr = group_events(mn, node, code);
+        if ((rc = upload(c, ev.data(), ev.size(), &T.ev))) return rc;
+        if ((rc = upload(c, eg.data(), eg.size(), &T.eg))) return rc;
+        if ((rc = upload(c, csr.ptr.data(), csr.ptr.size(), &T.csr_ptr))) return rc;
+        if ((rc = upload(c, csr.ent.data(), csr.ent.size(), &T.csr_ent))) return rc;
+        if ((rc = upload(c, m.boundary_nodes, (size_t)mn, &T.bnode))) return rc;
+        if ((rc = upload(c, m.CV_area, (size_t)mn, &T.cv))) return rc;
+        if ((rc = upload(c, m.vectors, 2 * (size_t)mn, &T.vec))) return rc;
+        if ((rc = upload(c, ebf.data(), ebf.size(), &T.eb_first))) return rc;
+        if ((rc = upload(c, ebc.data(), ebc.size(), &T.eb_count))) return rc;
+        if ((rc = upload(c, bv.data(), bv.size(), &T.b_v))) return rc;
+        if ((rc = upload(c, bn.data(), bn.size(), &T.b_n))) return rc;
+    }
+    void* p;
+    if ((rc = dev_alloc(c, sizeof(double) * 16 * (size_t)Ne, &p))) return rc;
+    P.contrib = (double*)p;
+    CK(cudaMemset(P.contrib, 0, sizeof(double) * 16 * (size_t)Ne));
+    if ((rc = dev_alloc(c, sizeof(int) * 4, &p))) return rc;
+    P.flag = (int*)p;
+    CK(cudaMemset(P.flag, 0, sizeof(int) * 4));
+    // launch shape of the cell kernel
+    P.micro_block = 128;
+    const size_t tab = sizeof(tsr_math_tables);
+    P.micro_smem = tab + sizeof(double) * (4 * (size_t)mn + 3 * (size_t)mNe + (size_t)T.nb + 16);
+    int dev_smem = 0, nsm = 0;
+    CK(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
+    if (P.micro_smem > (size_t)dev_smem) {
+        set_error("micro mesh too large for one cell in shared memory");
+        return TSR_ERR_ARG;
+    }
+    int occ = 1;
+    rc = tsr::configure_cell_kernels(P, &occ);
+    if (rc) return rc;
+    long long grid = (long long)occ * nsm;
+    P.micro_grid = (int)(grid < Ne ? grid : Ne);
+    if (P.micro_grid < 1) P.micro_grid = 1;
+    return TSR_OK;
+}
+
+int alloc_work(tsr_ctx* c, int max_krylov)
+{
+    const long long N = c->N;
+    void* p;
+    int rc;
+    double** vecs[] = {&c->d_u, &c->d_g0, &c->d_g1, &c->d_w, &c->d_unew, &c->d_winv, &c->d_x, &c->d_y};
+    for (double** v : vecs) {
+        if ((rc = dev_alloc(c, sizeof(double) * (size_t)N, &p))) return rc;
+        *v = (double*)p;
+    }
+    if ((rc = dev_alloc(c, sizeof(double) * ((size_t)c->Mn + c->Ne), &p))) return rc;
+    c->d_terms = (double*)p;
+    int maxk = max_krylov;
+    if (maxk > kMaxKrylovCap) maxk = kMaxKrylovCap;
+    if (maxk > N) maxk = (int)N;
+    if (maxk < 0) maxk = 0;
+    c->maxk = maxk;
+    c->ldH = maxk + 1;
+    if (maxk > 0) {
+        if ((rc = dev_alloc(c, sizeof(double) * (size_t)N * (size_t)(maxk + 1), &p))) return rc;
+        c->d_V = (double*)p;
+    }
+    const size_t nscal = (size_t)c->ldH * (size_t)(maxk > 0 ? maxk : 1) + S_COUNT;
+    if ((rc = dev_alloc(c, sizeof(double) * nscal, &p))) return rc;
+    c->d_scal = (double*)p;
+    CK(cudaMemset(c->d_scal, 0, sizeof(double) * nscal));
+    if ((rc = dev_alloc(c, sizeof(double) * 2 * (kMaxKrylovCap + 2), &p))) return rc;
+    c->d_coef = (double*)p;
+    c->d_z = c->d_coef + (kMaxKrylovCap + 2);
+    const int nb = reduction_blocks(N > (long long)c->Mn + c->Ne ? N : (long long)c->Mn + c->Ne);
+    if ((rc = dev_alloc(c, sizeof(double) * (size_t)nb, &p))) return rc;
+    c->rw.partials = (double*)p;
+    if ((rc = dev_alloc(c, sizeof(unsigned int) * 4, &p))) return rc;
+    c->rw.counter = (unsigned int*)p;
+    CK(cudaMemset(c->rw.counter, 0, sizeof(unsigned int) * 4));
+    CK(cudaMallocHost(&c->h_scal, sizeof(double) * nscal));
+    CK(cudaMallocHost(&c->h_coef, sizeof(double) * 2 * (kMaxKrylovCap + 2)));
+    CK(cudaMallocHost(&c->h_flag, sizeof(int) * 4));
+    c->Hm.assign((size_t)c->ldH * (size_t)(maxk > 0 ? maxk : 1), 0.0);
+    c->phi.assign((size_t)(maxk > 0 ? maxk : 1) * (size_t)(maxk > 0 ? maxk : 1), 0.0);
+    return TSR_OK;
+}
+
+int read_flag(tsr_ctx* c, int* flag)
+{
+    CK(cudaMemcpyAsync(c->h_flag, c->P.flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    *flag = c->h_flag[0];
+    return TSR_OK;
+}
+
+int reset_flag(tsr_ctx* c)
+{
+    CK(cudaMemsetAsync(c->P.flag, 0, sizeof(int), c->stream));
+    return TSR_OK;
+}
+
+int fetch_scalar(tsr_ctx* c, int slot, double* out)
+{
+    double* base = c->d_scal + (size_t)c->ldH * (size_t)(c->maxk > 0 ? c->maxk : 1);
+    CK(cudaMemcpyAsync(c->h_scal, base + slot, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    *out = c->h_scal[0];
+    return TSR_OK;
+}
+
+double* scal_slot(tsr_ctx* c, int slot)
+{
+    return c->d_scal + (size_t)c->ldH * (size_t)(c->maxk > 0 ? c->maxk : 1) + slot;
+}
+
+}  // namespace
+
+// ---- C-ABI ----------------------------------------------------------------
+
+extern "C" tsr_ctx* tsr_init(const user_data_struct* ud, const tsr_model_ext* ext, void* stream,
+                             int max_krylov)
+{
+    if (!ud) {
+        set_error("tsr_init: user_data is NULL");
+        return nullptr;
+    }
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev < 1) {
+        set_error(std::string("tsr_init: no CUDA device: ") + cudaGetErrorString(e));
+        return nullptr;
+    }
+    tsr_ctx* c = new tsr_ctx();
+    cudaGetDevice(&c->device);
+    if (stream) {
+        c->stream = (cudaStream_t)stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            set_error("tsr_init: cannot create stream");
+            delete c;
+            return nullptr;
+        }
+        c->own_stream = true;
+    }
+    int rc = build_problem(c, *ud, ext);
+    if (rc == TSR_OK) rc = alloc_work(c, max_krylov);
+    if (rc == TSR_OK && cudaDeviceSynchronize() != cudaSuccess) {
+        set_error("tsr_init: device error during set-up");
+        rc = TSR_ERR_CUDA;
+    }
+    if (rc != TSR_OK) {
+        tsr_free(c);
+        return nullptr;
+    }
+    return c;
+}
+
+extern "C" void tsr_free(tsr_ctx* c)
+{
+    if (!c) return;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (void* p : c->allocs) cudaFree(p);
+    if (c->h_scal) cudaFreeHost(c->h_scal);
+    if (c->h_coef) cudaFreeHost(c->h_coef);
+    if (c->h_flag) cudaFreeHost(c->h_flag);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+extern "C" void* tsr_stream(tsr_ctx* c) { return c ? (void*)c->stream : nullptr; }
+extern "C" int tsr_num_unknowns(tsr_ctx* c) { return c ? (int)c->N : 0; }
+
+extern "C" int tsr_g_eval_device(tsr_ctx* c, const double* d_u, double* d_g)
+{
+    if (!c || !d_u || !d_g) return TSR_ERR_ARG;
+    launch_g(c->P, 0, d_u, nullptr, nullptr, 0.0, 0.0, d_g, c->stream);
+    CK(cudaGetLastError());
+    return TSR_OK;
+}
+
+extern "C" int tsr_jv_device(tsr_ctx* c, const double* d_u, const double* d_g0, const double* d_v,
+                             double eps, double* d_w)
+{
+    if (!c || !d_u || !d_g0 || !d_v || !d_w || !(eps != 0.0)) return TSR_ERR_ARG;
+    launch_g(c->P, 1, d_u, d_v, d_g0, eps, 1.0 / eps, d_w, c->stream);
+    CK(cudaGetLastError());
+    return TSR_OK;
+}
+
+extern "C" int tsr_g_eval(tsr_ctx* c, const double* u, double* g)
+{
+    if (!c || !u || !g) return TSR_ERR_ARG;
+    const size_t bytes = sizeof(double) * (size_t)c->N;
+    int rc;
+    if ((rc = reset_flag(c))) return rc;
+    CK(cudaMemcpyAsync(c->d_x, u, bytes, cudaMemcpyHostToDevice, c->stream));
+    launch_g(c->P, 0, c->d_x, nullptr, nullptr, 0.0, 0.0, c->d_y, c->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(g, c->d_y, bytes, cudaMemcpyDeviceToHost, c->stream));
+    int flag = 0;
+    if ((rc = read_flag(c, &flag))) return rc;
+    if (flag) {
+        set_error("G: non-finite value");
+        return TSR_ERR_NAN;
+    }
+    return TSR_OK;
+}
+
+extern "C" int tsr_jv(tsr_ctx* c, const double* u, const double* g0, const double* v, double eps,
+                      double* w)
+{
+    if (!c || !u || !g0 || !v || !w || !(eps != 0.0)) return TSR_ERR_ARG;
+    const size_t bytes = sizeof(double) * (size_t)c->N;
+    CK(cudaMemcpyAsync(c->d_x, u, bytes, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_w, v, bytes, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_g1, g0, bytes, cudaMemcpyHostToDevice, c->stream));
+    launch_g(c->P, 1, c->d_x, c->d_w, c->d_g1, eps, 1.0 / eps, c->d_y, c->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(w, c->d_y, bytes, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return TSR_OK;
+}
+
+extern "C" int tsr_water_content(tsr_ctx* c, const double* u, double* water)
+{
+    if (!c || !u || !water) return TSR_ERR_ARG;
+    CK(cudaMemcpyAsync(c->d_x, u, sizeof(double) * (size_t)c->N, cudaMemcpyHostToDevice, c->stream));
+    launch_water(c->P, c->d_x, c->d_terms, scal_slot(c, S_WATER), c->rw, c->stream);
+    CK(cudaGetLastError());
+    return fetch_scalar(c, S_WATER, water);
+}
+
+extern "C" int tsr_dot(tsr_ctx* c, const double* x, const double* y, int n, double* out)
+{
+    if (!c || !x || !y || !out || n < 0 || n > c->N) return TSR_ERR_ARG;
+    const size_t bytes = sizeof(double) * (size_t)n;
+    CK(cudaMemcpyAsync(c->d_x, x, bytes, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_y, y, bytes, cudaMemcpyHostToDevice, c->stream));
+    launch_dot(c->d_x, c->d_y, n, scal_slot(c, S_DOT), c->rw, c->stream);
+    CK(cudaGetLastError());
+    return fetch_scalar(c, S_DOT, out);
+}
+
+// ---- EXPREM ------------------------------------------------------------------
+// The same algorithm, operation for operation, as the oracle's
+// oracle_exprem_step: see the description there and in the design notes.
+
+extern "C" int tsr_exprem_load(tsr_ctx* c, const double* u_host, double t)
+{
+    if (!c || !u_host) return TSR_ERR_ARG;
+    CK(cudaMemcpyAsync(c->d_u, u_host, sizeof(double) * (size_t)c->N, cudaMemcpyHostToDevice,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->state_loaded = true;
+    c->t_state = t;
+    c->g0_valid = false;
+    return TSR_OK;
+}
+
+extern "C" int tsr_exprem_store(tsr_ctx* c, double* u_host)
+{
+    if (!c || !u_host || !c->state_loaded) return TSR_ERR_ARG;
+    CK(cudaMemcpyAsync(u_host, c->d_u, sizeof(double) * (size_t)c->N, cudaMemcpyDeviceToHost,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return TSR_OK;
+}
+
+namespace {
+
+int upload_coef(tsr_ctx* c, const double* v, int n, double* dst)
+{
+    std::memcpy(c->h_coef, v, sizeof(double) * (size_t)n);
+    CK(cudaMemcpyAsync(dst, c->h_coef, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+    // the pinned staging buffer is reused by the next upload: wait for it
+    CK(cudaStreamSynchronize(c->stream));
+    return TSR_OK;
+}
+
+int phi_host(tsr_ctx* c, double alpha, int m)
+{
+    int rc = phipade_host(c->phi.data(), c->Hm.data(), alpha, m, c->ldH, c->maxk);
+    if (rc) set_error("phipade: singular Pade denominator");
+    return rc;
+}
+
+}  // namespace
+
+extern "C" int tsr_exprem_advance(tsr_ctx* c, double tend, const double* tspan, double* tspan_solns,
+                                  const exprem_options_struct* opt, exprem_stats_struct* st,
+                                  double* t_out)
+{
+    if (!c || !opt || !st || !tspan || !c->state_loaded) return TSR_ERR_ARG;
+    if (c->maxk < 1) {
+        set_error("context created without a Krylov basis (max_krylov = 0)");
+        return TSR_ERR_ARG;
+    }
+    const long long N = c->N;
+    const size_t bytes = sizeof(double) * (size_t)N;
+    int maxk = opt->MaxKrylov < (int)N ? opt->MaxKrylov : (int)N;
+    if (maxk > c->maxk) maxk = c->maxk;
+    const int ldH = c->ldH;
+    double t = c->t_state;
+    if (t == 0.0) {
+        st->NumSteps = 0;
+        st->FuncEvals = 0;
+        st->CurrentStep = opt->InitStep;
+        st->CurrentKryDim = 0;
+        st->CurrentTime = 0.0;
+        c->g0_valid = false;
+    }
+    if (st->NumSteps >= opt->MaxNumSteps) {
+        set_error("MaxNumSteps reached");
+        return TSR_ERR_MAXSTEPS;
+    }
+    double dt = st->CurrentStep;
+    if (dt > opt->MaxStep) dt = opt->MaxStep;
+    bool last = false;
+    if (t + dt >= tend) {
+        dt = tend - t;
+        last = true;
+    }
+    int rc;
+    cudaStream_t s = c->stream;
+    double* V = c->d_V;
+    double* Hd = c->d_scal;   // Hessenberg block, column j at j*ldH
+    if (!c->g0_valid) {
+        if ((rc = reset_flag(c))) return rc;
+        launch_g(c->P, 0, c->d_u, nullptr, nullptr, 0.0, 0.0, c->d_g0, s);
+        CK(cudaGetLastError());
+        st->FuncEvals++;
+        int flag = 0;
+        if ((rc = read_flag(c, &flag))) return rc;
+        if (flag) {
+            set_error("G(u) non-finite at the current state");
+            return TSR_ERR_GFUNC;
+        }
+        c->g0_valid = true;
+    }
+    std::fill(c->Hm.begin(), c->Hm.end(), 0.0);
+    launch_winv(c->d_u, opt->RelTol, opt->AbsTol, c->d_winv, N, s);
+    launch_dot(c->d_g0, c->d_g0, N, scal_slot(c, S_BETA2), c->rw, s);
+    launch_dot(c->d_u, c->d_u, N, scal_slot(c, S_NU2), c->rw, s);
+    CK(cudaGetLastError());
+    double b2, n2;
+    if ((rc = fetch_scalar(c, S_BETA2, &b2))) return rc;
+    if ((rc = fetch_scalar(c, S_NU2, &n2))) return rc;
+    const double beta = std::sqrt(b2);
+    const double nu = std::sqrt(n2);
+    const double eps = std::sqrt((1.0 + nu) * DBL_EPSILON);
+    int m = 0;
+    bool happy = false;
+    double errK = 0.0, vnw = 0.0;
+    if (beta != 0.0) {
+        const double ib = 1.0 / beta;
+        launch_scale(c->d_g0, ib, V, N, s);
+        for (int j = 0; j < maxk; ++j) {
+            const double* vj = V + (size_t)j * N;
+            launch_g(c->P, 1, c->d_u, vj, c->d_g0, eps, 1.0 / eps, c->d_w, s);
+            st->FuncEvals++;
+            double* Hc = Hd + (size_t)j * ldH;
+            launch_dot(c->d_w, V, N, Hc, c->rw, s);
+            for (int i = 0; i <= j; ++i) {
+                const double* vnext = (i < j) ? V + (size_t)(i + 1) * N : nullptr;
+                double* res = (i < j) ? Hc + i + 1 : scal_slot(c, S_HSQ);
+                launch_mgs(c->d_w, V + (size_t)i * N, Hc + i, vnext, N, res, c->rw, s);
+            }
+            double* vn = V + (size_t)(j + 1) * N;
+            launch_scale_wsq(c->d_w, scal_slot(c, S_HSQ), Hc + j + 1, scal_slot(c, S_IH), vn,
+                             c->d_winv, N, scal_slot(c, S_SV), c->rw, s);
+            CK(cudaGetLastError());
+            // column j of H and the weighted norm of v_{j+1}
+            CK(cudaMemcpyAsync(c->h_scal, Hc, sizeof(double) * (size_t)(j + 2), cudaMemcpyDeviceToHost, s));
+            CK(cudaMemcpyAsync(c->h_scal + ldH, scal_slot(c, S_SV), sizeof(double), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            double hs = 0.0;
+            for (int i = 0; i <= j; ++i) {
+                const double hij = c->h_scal[i];
+                c->Hm[(size_t)j * ldH + i] = hij;
+                hs = std::fma(hij, hij, hs);
+            }
+            const double hn = c->h_scal[j + 1];
+            c->Hm[(size_t)j * ldH + j + 1] = hn;
+            const double Sv = c->h_scal[ldH];
+            m = j + 1;
+            if (!(hn > 1e-12 * std::sqrt(std::fma(hn, hn, hs)))) {
+                happy = true;
+                break;
+            }
+            if (m < opt->MinKrylov && m < maxk) continue;
+            vnw = std::sqrt(Sv / (double)N);
+            if ((rc = phi_host(c, dt, m))) return rc;
+            errK = std::fabs(((dt * beta) * hn) * c->phi[m - 1]) * vnw;
+            if (errK <= kKrylovTol) break;
+        }
+        if (!happy && errK > kKrylovTol) {
+            while (errK > kKrylovTol) {
+                const double f = 0.5 > opt->MinStepDecFac ? 0.5 : opt->MinStepDecFac;
+                dt = dt * f;
+                last = false;
+                if (dt < opt->MinStep) {
+                    set_error("step size below MinStep (Krylov)");
+                    return TSR_ERR_MINSTEP;
+                }
+                if ((rc = phi_host(c, dt, m))) return rc;
+                errK = std::fabs(((dt * beta) * c->Hm[(size_t)(m - 1) * ldH + m]) * c->phi[m - 1]) * vnw;
+            }
+        }
+    }
+    std::vector<double> cv((size_t)kMaxKrylovCap + 1), z((size_t)kMaxKrylovCap + 2);
+    for (;;) {
+        if (m > 0) {
+            if ((rc = phi_host(c, dt, m))) return rc;
+            const double dtb = dt * beta;
+            for (int i = 0; i < m; ++i) cv[i] = dtb * c->phi[i];
+            if ((rc = upload_coef(c, cv.data(), m, c->d_coef))) return rc;
+            launch_combine(c->d_u, V, N, c->d_coef, m, c->d_unew, N, s);
+        } else {
+            CK(cudaMemcpyAsync(c->d_unew, c->d_u, bytes, cudaMemcpyDeviceToDevice, s));
+        }
+        if ((rc = reset_flag(c))) return rc;
+        launch_g(c->P, 0, c->d_unew, nullptr, nullptr, 0.0, 0.0, c->d_g1, s);
+        st->FuncEvals++;
+        double err = 0.0;
+        int mz = 0;
+        if (m > 0) {
+            mz = happy ? m : m + 1;
+            for (int i = 0; i < mz; ++i) {
+                double a = 0.0;
+                for (int k = 0; k < m; ++k) a = std::fma(c->Hm[(size_t)k * ldH + i], cv[k], a);
+                z[i] = a;
+            }
+            if ((rc = upload_coef(c, z.data(), mz, c->d_z))) return rc;
+            launch_err(c->d_g1, c->d_g0, V, N, c->d_z, mz, dt / 3.0, c->d_winv, N, scal_slot(c, S_ERR),
+                       c->rw, s);
+        }
+        CK(cudaGetLastError());
+        int flag = 0;
+        if ((rc = read_flag(c, &flag))) return rc;
+        if (flag) {
+            err = INFINITY;
+        } else if (m > 0) {
+            double S;
+            if ((rc = fetch_scalar(c, S_ERR, &S))) return rc;
+            err = std::sqrt(S / (double)N);
+        }
+        if (err <= 1.0) {
+            const int ns = (int)tspan[0];
+            const double tn = last ? tend : t + dt;
+            for (int k = 1; k <= ns; ++k) {
+                if (tspan[k] > t && tspan[k] <= tn && tspan_solns) {
+                    double* row = tspan_solns + (size_t)k * (size_t)N;
+                    if (m == 0) {
+                        CK(cudaMemcpyAsync(row, c->d_u, bytes, cudaMemcpyDeviceToHost, s));
+                    } else {
+                        const double tau = tspan[k] - t;
+                        if ((rc = phi_host(c, tau, m))) return rc;
+                        const double tb = tau * beta;
+                        std::vector<double> cd((size_t)m);
+                        for (int i = 0; i < m; ++i) cd[i] = tb * c->phi[i];
+                        if ((rc = upload_coef(c, cd.data(), m, c->d_coef))) return rc;
+                        launch_combine(c->d_u, V, N, c->d_coef, m, c->d_x, N, s);
+                        CK(cudaMemcpyAsync(row, c->d_x, bytes, cudaMemcpyDeviceToHost, s));
+                    }
+                    CK(cudaStreamSynchronize(s));
+                }
+            }
+            std::swap(c->d_u, c->d_unew);
+            std::swap(c->d_g0, c->d_g1);
+            t = tn;
+            double fac = (err > 0.0) ? opt->SafetyFac * std::pow(err, -1.0 / 3.0) : opt->MaxStepIncFac;
+            if (fac > opt->MaxStepIncFac) fac = opt->MaxStepIncFac;
+            if (fac < opt->MinStepDecFac) fac = opt->MinStepDecFac;
+            double dn = dt * fac;
+            if (dn > opt->MaxStep) dn = opt->MaxStep;
+            if (dn < opt->MinStep) dn = opt->MinStep;
+            st->CurrentStep = dn;
+            st->CurrentTime = t;
+            st->CurrentKryDim = m;
+            st->NumSteps++;
+            c->t_state = t;
+            c->g0_valid = true;
+            if (t_out) *t_out = t;
+            return TSR_OK;
+        }
+        double fac = (err == err && err < INFINITY) ? opt->SafetyFac * std::pow(err, -1.0 / 3.0)
+                                                     : opt->MinStepDecFac;
+        if (fac < opt->MinStepDecFac) fac = opt->MinStepDecFac;
+        if (fac > 1.0) fac = opt->MinStepDecFac;
+        dt = dt * fac;
+        last = false;
+        if (dt < opt->MinStep) {
+            set_error("step size below MinStep");
+            return TSR_ERR_MINSTEP;
+        }
+    }
+}
+
+extern "C" int tsr_exprem_step(tsr_ctx* c, double* t, double tend, const double* tspan,
+                               double* tspan_solns, double* u0, const exprem_options_struct* opt,
+                               exprem_stats_struct* st)
+{
+    if (!c || !t || !u0 || !opt || !st || !tspan) return TSR_ERR_ARG;
+    // reuse G(u) of the previous accepted step when the caller hands back
+    // the same state (same array, same time)
+    const bool cached = c->state_loaded && c->g0_valid && c->last_u0 == u0 && c->last_t == *t &&
+                        *t != 0.0;
+    int rc;
+    if (cached) {
+        CK(cudaMemcpyAsync(c->d_u, u0, sizeof(double) * (size_t)c->N, cudaMemcpyHostToDevice,
+                           c->stream));
+        c->t_state = *t;
+    } else {
+        if ((rc = tsr_exprem_load(c, u0, *t))) return rc;
+    }
+    st->CurrentSoln = u0;
+    double tn = *t;
+    rc = tsr_exprem_advance(c, tend, tspan, tspan_solns, opt, st, &tn);
+    if (rc != TSR_OK) return rc;
+    if ((rc = tsr_exprem_store(c, u0))) return rc;
+    *t = tn;
+    c->last_u0 = u0;
+    c->last_t = tn;
+    return TSR_OK;
+}
+
+// ---- implicit contexts of the drop-in entry points ---------------------------
+namespace {
+std::mutex g_reg_mu;
+std::map<const void*, tsr_ctx*> g_reg;
+tsr_model_ext g_default_ext{};
+bool g_have_ext = false;
+int g_default_maxk = 100;
+}  // namespace
+
+namespace tsr {
+tsr_ctx* registry_get(const user_data_struct* ud, int* rc)
+{
+    std::lock_guard<std::mutex> lk(g_reg_mu);
+    const void* key = ud->macro_mesh.elements;
+    auto it = g_reg.find(key);
+    if (it != g_reg.end()) {
+        *rc = TSR_OK;
+        return it->second;
+    }
+    tsr_ctx* c = tsr_init(ud, g_have_ext ? &g_default_ext : nullptr, nullptr, g_default_maxk);
+    if (!c) {
+        *rc = TSR_ERR_CUDA;
+        return nullptr;
+    }
+    g_reg[key] = c;
+    *rc = TSR_OK;
+    return c;
+}
+}  // namespace tsr
+
+extern "C" int tsr_set_default_ext(const tsr_model_ext* ext, int max_krylov)
+{
+    std::lock_guard<std::mutex> lk(g_reg_mu);
+    if (ext) {
+        g_default_ext = *ext;
+        g_have_ext = true;
+    } else {
+        g_have_ext = false;
+    }
+    if (max_krylov > 0) g_default_maxk = max_krylov;
+    return TSR_OK;
+}
+
+extern "C" void tsr_release_all(void)
+{
+    std::lock_guard<std::mutex> lk(g_reg_mu);
+    for (auto& kv : g_reg) tsr_free(kv.second);
+    g_reg.clear();
+}
+
+extern "C" int tsr_gfunc_gpu(double* g, double* u, const user_data_struct* ud)
+{
+    if (!g || !u || !ud) return TSR_ERR_ARG;
+    int rc;
+    tsr_ctx* c = tsr::registry_get(ud, &rc);
+    if (!c) return rc;
+    return tsr_g_eval(c, u, g);
+}

@@ -1,0 +1,115 @@
+// tsr_device.h -- device-side data of one problem and the kernel launchers
+// (host-callable).  Only the library's own translation units include this.
+#ifndef TSR_DEVICE_H
+#define TSR_DEVICE_H
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace tsr {
+
+// Van Genuchten parameters with the derived constants the kernels use.
+struct VGPar {
+    double Ks, thr, ths, alpha, n, m;
+    double dth, coefC, mh;
+};
+
+// Micro-cell template: the reference's one shared micro mesh
+// (include/user_data.h:4) re-laid out for the cell kernel.
+struct MicroTpl {
+    int mn, mNe, nb;
+    int pad;
+    const int* ev;          // [3*mNe]  vertices of element e at 3e+j
+    const double* eg;       // [12*mNe] per element: sfx0..2, sfy0..2, nx0, ny0, nx1, ny1, nx2, ny2
+    const int* csr_ptr;     // [mn+1]
+    const int* csr_ent;     // (3e+j)<<1 | (1 if subtracted)
+    const int* bnode;       // [mn]
+    const double* cv;       // [mn]
+    const double* vec;      // [2*mn] x block then y block
+    const int* eb_first;    // [mNe] first boundary item of element e
+    const int* eb_count;    // [mNe]
+    const int* b_v;         // [nb] node of item
+    const double* b_n;      // [2*nb] outward length-weighted normal of item
+};
+
+// Macro mesh in the reference layout plus derived arrays.
+struct MacroDev {
+    int Mn, Ne, nv;
+    int pad;
+    const int* elements;    // [nv*Ne]
+    const double* sf;       // [nv*nv*Ne]
+    const double* normals;  // [2*nv*Ne]
+    const double* midx;
+    const double* midy;
+    const int* bce;         // [nv*Ne]
+    const double* blen;     // [2*nv*Ne]
+    const double* bmid;     // [4*nv*Ne]
+    const double* bnrm;     // [4*nv*Ne]
+    const double* scv;      // [nv*Ne]
+    const double* cv;       // [Mn]
+    const double* cent;     // [2*Ne]
+    const unsigned char* dirichlet;  // [Mn]
+    const int* csr_ptr;     // [Mn+1]
+    const int* csr_ent;     // (16k+slot)<<1 | neg
+    const double* keff;     // [4*nk]
+    int nk;
+    int model_type;
+    double keff_first, keff_inv_logr;
+    double epsA, inv_Y, Ss, bflux;
+};
+
+struct Problem {
+    MacroDev M;
+    MicroTpl m;
+    VGPar pA, pB;
+    const double* cell_scale;   // [Ne] or nullptr
+    int kface;
+    int micro_block;            // threads per cell CTA
+    size_t micro_smem;          // dynamic shared memory per cell CTA
+    int micro_grid;             // persistent grid of the cell kernel
+    double* contrib;            // [16*Ne] macro contributions per element
+    int* flag;                  // device word: bit 0 non-finite G
+    long long N;
+};
+
+// Opt the cell kernel into its dynamic shared memory and report how many
+// of its CTAs fit on one SM.  Returns 0 on success.
+int configure_cell_kernels(const Problem& P, int* occ);
+
+// Two-scale G (mode 0) or finite-difference Jv (mode 1):
+//   mode 0: out = G(u)
+//   mode 1: out = (G(u + eps v) - g0) * inv_eps
+void launch_g(const Problem& P, int mode, const double* u, const double* v, const double* g0,
+              double eps, double inv_eps, double* out, cudaStream_t s);
+
+// Fixed-order reductions (result written to device scalar *res).
+struct RedWork {
+    double* partials;       // [nblocks]
+    unsigned int* counter;  // one word per concurrent reduction slot
+};
+int reduction_blocks(long long n);
+void launch_dot(const double* x, const double* y, long long n, double* res, RedWork w, cudaStream_t s);
+void launch_wsq(const double* x, const double* winv, long long n, double* res, RedWork w, cudaStream_t s);
+void launch_vsum(const double* x, long long n, double* res, RedWork w, cudaStream_t s);
+// w <- fma(-(*h), vi, w) and *res = dot(w, vnext) (or dot(w, w) if vnext is null)
+void launch_mgs(double* w, const double* vi, const double* h, const double* vnext, long long n,
+                double* res, RedWork rw, cudaStream_t s);
+// *hn = sqrt(*hsq), *ih = 1 / *hn; v = w * (*ih); *res = sum (v winv)^2
+void launch_scale_wsq(const double* w, const double* hsq, double* hn, double* ih, double* v,
+                      const double* winv, long long n, double* res, RedWork rw, cudaStream_t s);
+void launch_scale(const double* x, double a, double* y, long long n, cudaStream_t s);
+void launch_winv(const double* u, double rtol, double atol, double* winv, long long n, cudaStream_t s);
+// out = u + sum_i c[i] V_i
+void launch_combine(const double* u, const double* V, long long ldV, const double* c, int m,
+                    double* out, long long n, cudaStream_t s);
+// res = sum ((g1 - g0 - sum_i z_i V_i) * dt3 * winv)^2
+void launch_err(const double* g1, const double* g0, const double* V, long long ldV, const double* z,
+                int mz, double dt3, const double* winv, long long n, double* res, RedWork rw,
+                cudaStream_t s);
+// total water content
+void launch_water(const Problem& P, const double* u, double* terms, double* res, RedWork rw,
+                  cudaStream_t s);
+
+}  // namespace tsr
+
+#endif

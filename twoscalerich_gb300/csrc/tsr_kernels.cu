@@ -1,0 +1,698 @@
+// tsr_kernels.cu -- sm_103a kernels of the two-scale Richards hot path.
+//
+// Everything is FP64.  On GB300 the FP64 pipe (measured 0.50 Top/s for
+// DFMA, DADD and DMUL alike) is ~70x slower than HBM per byte of the right-
+// hand side, so the kernels are organised around FP64 instruction count:
+//   * one persistent CTA per SM slot walks the micro cells; a cell's heads,
+//     half-conductivities and face fluxes live in shared memory, and each
+//     node gathers its face fluxes from a precomputed list (no atomics, a
+//     fixed summation order, hence results independent of scheduling);
+//   * elementary functions are the table-driven tsr_math.h routines (14
+//     FP64 ops for log, 11 for exp, about half of the device libm's cost),
+//     with their tables copied into shared memory once per CTA;
+//   * transcendentals are evaluated once per node, never per face;
+//   * the macro element terms ride on the CTA of the element's cell (cell k
+//     belongs to macro element k), so one G costs two launches.
+// All reductions use one fixed order (described with the oracle and in the
+// design notes); the finite-difference Jv, the Gram-Schmidt coefficients
+// and the step-error norm are therefore reproducible bit for bit.
+//
+// The code is compiled with -fmad=false: every fused multiply-add is an
+// explicit fma(), matching the host evaluation operation for operation.
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "tsr_device.h"
+#include "tsr_internal.h"
+#include "tsr_math.h"
+
+namespace tsr {
+
+__device__ const tsr_math_tables d_tables = TSR_MATH_TABLES_INIT;
+
+static constexpr int kTabDoubles = (int)(sizeof(tsr_math_tables) / sizeof(double));
+
+__device__ __forceinline__ void load_tables(tsr_math_tables* s)
+{
+    const double2* src = reinterpret_cast<const double2*>(&d_tables);
+    double2* dst = reinterpret_cast<double2*>(s);
+    for (int i = threadIdx.x; i < (int)(sizeof(tsr_math_tables) / 16); i += blockDim.x) dst[i] = src[i];
+}
+
+__device__ __forceinline__ bool finite_d(double x)
+{
+    return (tsr_d2u(x) & TSR_ABS_MASK) < TSR_INF_BITS;
+}
+
+// ---- van Genuchten-Mualem (same operation sequence as the host oracle) ---
+__device__ __forceinline__ void vg_full(double h, const VGPar& p, const tsr_math_tables* T,
+                                        double& K, double& Cn, double& Cd)
+{
+    if (h < 0.0) {
+        double ah = -h;
+        double a = p.alpha * ah;
+        double L = tsr_log(a, T);
+        double nL = p.n * L;
+        double t = tsr_exp(nL, T);
+        double s1 = 1.0 + t;
+        double l1 = tsr_log1p_s(t, s1, T);
+        double X = tsr_exp(p.mh * l1, T);
+        double Se = X * X;
+        double B = -tsr_expm1(p.m * (nL - l1), T);
+        K = (p.Ks * X) * (B * B);
+        Cn = p.coefC * (t * Se);
+        Cd = ah * s1;
+    } else {
+        K = p.Ks;
+        Cn = 0.0;
+        Cd = 1.0;
+    }
+}
+
+__device__ __forceinline__ void vg_storage(double h, const VGPar& p, const tsr_math_tables* T,
+                                           double& Cn, double& Cd)
+{
+    if (h < 0.0) {
+        double ah = -h;
+        double a = p.alpha * ah;
+        double L = tsr_log(a, T);
+        double nL = p.n * L;
+        double t = tsr_exp(nL, T);
+        double s1 = 1.0 + t;
+        double l1 = tsr_log1p_s(t, s1, T);
+        double X = tsr_exp(p.mh * l1, T);
+        double Se = X * X;
+        Cn = p.coefC * (t * Se);
+        Cd = ah * s1;
+    } else {
+        Cn = 0.0;
+        Cd = 1.0;
+    }
+}
+
+__device__ __forceinline__ double vg_se(double h, const VGPar& p, const tsr_math_tables* T)
+{
+    if (!(h < 0.0)) return 1.0;
+    double ah = -h;
+    double a = p.alpha * ah;
+    double L = tsr_log(a, T);
+    double nL = p.n * L;
+    double t = tsr_exp(nL, T);
+    double s1 = 1.0 + t;
+    double l1 = tsr_log1p_s(t, s1, T);
+    double X = tsr_exp(p.mh * l1, T);
+    return X * X;
+}
+
+// ---- effective conductivity table --------------------------------------
+__device__ __forceinline__ void keff_dev(double H, const MacroDev& M, const tsr_math_tables* T,
+                                         double K[4])
+{
+    const int n = M.nk;
+    if (n < 2) {
+        for (int c = 0; c < 4; ++c) K[c] = M.keff[c * n];
+        return;
+    }
+    double x = tsr_log(fabs(H), T) * TSR_INV_LN10;
+    double pos = (x - M.keff_first) * M.keff_inv_logr;
+    int i;
+    double w;
+    if (!(pos > 0.0)) {
+        i = 0;
+        w = 0.0;
+    } else if (pos >= (double)(n - 1)) {
+        i = n - 2;
+        w = 1.0;
+    } else {
+        i = (int)pos;
+        w = pos - (double)i;
+    }
+    for (int c = 0; c < 4; ++c) {
+        double k0 = __ldg(M.keff + c * n + i), k1 = __ldg(M.keff + c * n + i + 1);
+        K[c] = fma(w, k1 - k0, k0);
+    }
+}
+
+__device__ __forceinline__ double interp_at(int nv, const double* al, double x, double y)
+{
+    if (nv == 3) return fma(al[0], x, fma(al[1], y, al[2]));
+    return fma(al[0], x, fma(al[1], y, fma(al[2], x * y, al[3])));
+}
+
+__device__ __forceinline__ void interp_grad(int nv, const double* al, double x, double y,
+                                            double& gx, double& gy)
+{
+    if (nv == 3) {
+        gx = al[0];
+        gy = al[1];
+    } else {
+        gx = fma(al[2], y, al[0]);
+        gy = fma(al[2], x, al[1]);
+    }
+}
+
+template <int MODE>
+__device__ __forceinline__ double state_at(const double* __restrict__ u, const double* __restrict__ v,
+                                           double eps, long long i)
+{
+    if (MODE == 0) return u[i];
+    return fma(eps, v[i], u[i]);
+}
+
+// Macro element k's contributions (faces, boundary sub-edges, exchange),
+// one per lane of warp 0.  Slot layout per element: [0,nv) faces,
+// [nv,3nv) boundary halves (2j+s), [3nv,4nv) exchange.
+__device__ __forceinline__ void macro_element_terms(const Problem& P, int k, const double* al, double Q,
+                                    const tsr_math_tables* T, int lane)
+{
+    const MacroDev& M = P.M;
+    const int nv = M.nv, Ne = M.Ne;
+    double* out = P.contrib + (long long)16 * k;
+    if (lane < nv) {
+        const int j = lane;
+        double mx = M.midx[(long long)j * Ne + k], my = M.midy[(long long)j * Ne + k];
+        double gx, gy;
+        interp_grad(nv, al, mx, my, gx, gy);
+        double Hf = interp_at(nv, al, mx, my);
+        double K[4];
+        keff_dev(Hf, M, T, K);
+        double gy1 = gy + 1.0;
+        double qx = fma(K[0], gx, K[1] * gy1);
+        double qy = fma(K[2], gx, K[3] * gy1);
+        double nx = M.normals[(long long)(2 * j) * Ne + k];
+        double ny = M.normals[(long long)(2 * j + 1) * Ne + k];
+        out[j] = fma(qx, nx, qy * ny);
+    } else if (lane < 3 * nv) {
+        const int q = lane - nv, j = q >> 1, sh = q & 1;
+        const int bc = M.bce[(long long)j * Ne + k];
+        if (bc == 1) {
+            out[nv + q] = M.bflux * M.blen[(long long)(2 * j + sh) * Ne + k];
+        } else if (bc == 3 || bc == 4) {
+            double bx = M.bmid[(long long)(4 * j + 2 * sh) * Ne + k];
+            double by = M.bmid[(long long)(4 * j + 2 * sh + 1) * Ne + k];
+            double gx, gy;
+            interp_grad(nv, al, bx, by, gx, gy);
+            if (bc == 3) gx = 0.0;
+            if (bc == 4) gy = 0.0;
+            double Hb = interp_at(nv, al, bx, by);
+            double K[4];
+            keff_dev(Hb, M, T, K);
+            double gy1 = gy + 1.0;
+            double qx = fma(K[0], gx, K[1] * gy1);
+            double qy = fma(K[2], gx, K[3] * gy1);
+            double nbx = M.bnrm[(long long)(4 * j + 2 * sh) * Ne + k];
+            double nby = M.bnrm[(long long)(4 * j + 2 * sh + 1) * Ne + k];
+            out[nv + q] = fma(qx, nbx, qy * nby);
+        }
+    } else if (lane < 4 * nv) {
+        if (M.model_type == 3) {
+            const int j = lane - 3 * nv;
+            out[3 * nv + j] = M.scv[(long long)j * Ne + k] * (Q * M.inv_Y);
+        }
+    }
+}
+
+// ---- the micro-cell kernel ----------------------------------------------
+// Dynamic shared memory: tables | h[mn] | Kh[mn] | Cd[mn] | den[mn] |
+// F[3 mNe] | items[nb] | misc[16] (interpolant coefficients, vertex heads).
+template <int MODE>
+__global__ void __launch_bounds__(128) k_cells(Problem P, const double* __restrict__ u,
+                                               const double* __restrict__ v,
+                                               const double* __restrict__ g0, double eps,
+                                               double inv_eps, double* __restrict__ out)
+{
+    extern __shared__ double sm[];
+    tsr_math_tables* T = reinterpret_cast<tsr_math_tables*>(sm);
+    const int mn = P.m.mn, mNe = P.m.mNe, nb = P.m.nb;
+    double* h = sm + kTabDoubles;
+    double* Kh = h + mn;
+    double* Cd = Kh + mn;
+    double* den = Cd + mn;
+    double* F = den + mn;
+    double* items = F + 3 * mNe;
+    double* misc = items + nb;
+    const int tid = threadIdx.x, bs = blockDim.x;
+    const int lane = tid & 31;
+    const MacroDev& M = P.M;
+    const int nv = M.nv, Ne = M.Ne;
+    const bool exch = (M.model_type == 3);
+    load_tables(T);
+    int bad = 0;
+    for (int k = blockIdx.x; k < Ne; k += gridDim.x) {
+        __syncthreads();
+        if (tid < 32) {
+            // vertex heads, then interpolant coefficients of element k
+            if (lane < nv) misc[8 + lane] = state_at<MODE>(u, v, eps, M.elements[(long long)lane * Ne + k]);
+            __syncwarp();
+            if (lane < nv) {
+                const int m = lane;
+                double a = M.sf[(long long)(m * nv + 0) * Ne + k] * misc[8];
+                for (int i = 1; i < nv; ++i)
+                    a = fma(M.sf[(long long)(m * nv + i) * Ne + k], misc[8 + i], a);
+                misc[m] = a;
+            }
+        }
+        __syncthreads();
+        const long long off = (long long)M.Mn + (long long)k * mn;
+        const double s = P.cell_scale ? P.cell_scale[k] : 1.0;
+        const double s2 = s * s;
+        const double cx = M.cent[k], cy = M.cent[Ne + k];
+        // nodes: head, conductivity, storage
+        for (int l = tid; l < mn; l += bs) {
+            const bool bnd = P.m.bnode[l] != 0;
+            double hl;
+            if (bnd) {
+                double px = cx, py = cy;
+                if (M.model_type != 1) {
+                    px = fma(s, P.m.vec[l], cx);
+                    py = fma(s, P.m.vec[mn + l], cy);
+                }
+                hl = interp_at(nv, misc, px, py);
+            } else {
+                hl = state_at<MODE>(u, v, eps, off + l);
+            }
+            h[l] = hl;
+            double K, Cn, Cdl;
+            vg_full(hl, P.pB, T, K, Cn, Cdl);
+            Kh[l] = 0.5 * K;
+            Cd[l] = Cdl;
+            den[l] = fma(M.Ss, Cdl, Cn) * (P.m.cv[l] * s2);
+        }
+        __syncthreads();
+        // elements: SCV face fluxes and inclusion-boundary exchange items
+        for (int e = tid; e < mNe; e += bs) {
+            const int v0 = P.m.ev[3 * e], v1 = P.m.ev[3 * e + 1], v2 = P.m.ev[3 * e + 2];
+            const double* G = P.m.eg + 12 * (long long)e;
+            const double h0 = h[v0], h1 = h[v1], h2 = h[v2];
+            double gx = G[0] * h0;
+            gx = fma(G[1], h1, gx);
+            gx = fma(G[2], h2, gx);
+            double gy = G[3] * h0;
+            gy = fma(G[4], h1, gy);
+            gy = fma(G[5], h2, gy);
+            const double gys = gy + s;
+            const int vv[3] = {v0, v1, v2};
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const int a = vv[j], b = vv[(j + 1) % 3];
+                double dot = fma(gx, G[6 + 2 * j], gys * G[7 + 2 * j]);
+                double Kf;
+                if (P.kface == 1)
+                    Kf = (dot > 0.0) ? (2.0 * Kh[b]) : (2.0 * Kh[a]);
+                else
+                    Kf = Kh[a] + Kh[b];
+                F[3 * e + j] = Kf * dot;
+            }
+            if (exch) {
+                const int c = P.m.eb_count[e];
+                if (c > 0) {
+                    const int f0 = P.m.eb_first[e];
+                    for (int q = 0; q < c; ++q) {
+                        const int it = f0 + q;
+                        items[it] = (2.0 * Kh[P.m.b_v[it]]) *
+                                    fma(gx, P.m.b_n[2 * it], gys * P.m.b_n[2 * it + 1]);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        // nodes: gather face fluxes in the fixed order, divide by storage
+        for (int l = tid; l < mn; l += bs) {
+            double g;
+            if (P.m.bnode[l]) {
+                g = 0.0;
+            } else {
+                double acc = 0.0;
+                const int p1 = P.m.csr_ptr[l + 1];
+                for (int p = P.m.csr_ptr[l]; p < p1; ++p) {
+                    const int ent = P.m.csr_ent[p];
+                    const double f = F[ent >> 1];
+                    acc = (ent & 1) ? (acc - f) : (acc + f);
+                }
+                g = (acc * Cd[l]) / den[l];
+            }
+            if (!finite_d(g)) bad = 1;
+            if (MODE == 0)
+                out[off + l] = g;
+            else
+                out[off + l] = (g - g0[off + l]) * inv_eps;
+        }
+        // exchange flux and the macro element terms (warp 0)
+        if (tid < 32) {
+            double Q = 0.0;
+            if (exch) {
+                double p = 0.0;
+                for (int i = lane; i < nb; i += 32) p = p + items[i];
+#pragma unroll
+                for (int d = 16; d >= 1; d >>= 1) p = p + __shfl_xor_sync(0xffffffffu, p, d);
+                Q = p;
+            }
+            macro_element_terms(P, k, misc, Q, T, lane);
+        }
+    }
+    if (bad) atomicOr(P.flag, 1);
+}
+
+// ---- macro nodes ----------------------------------------------------------
+template <int MODE>
+__global__ void __launch_bounds__(128) k_macro_nodes(Problem P, const double* __restrict__ u,
+                                                     const double* __restrict__ v,
+                                                     const double* __restrict__ g0, double eps,
+                                                     double inv_eps, double* __restrict__ out)
+{
+    __shared__ tsr_math_tables T;
+    load_tables(&T);
+    __syncthreads();
+    const MacroDev& M = P.M;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M.Mn) return;
+    double g;
+    if (M.dirichlet[i]) {
+        g = 0.0;
+    } else {
+        const double H = state_at<MODE>(u, v, eps, i);
+        double acc = 0.0;
+        const int p1 = M.csr_ptr[i + 1];
+        for (int p = M.csr_ptr[i]; p < p1; ++p) {
+            const int ent = M.csr_ent[p];
+            const double c = P.contrib[ent >> 1];
+            acc = (ent & 1) ? (acc - c) : (acc + c);
+        }
+        double Cn, Cd;
+        vg_storage(H, P.pA, &T, Cn, Cd);
+        const double A = M.epsA * M.cv[i];
+        const double den = fma(M.Ss, Cd, Cn) * A;
+        g = (acc * Cd) / den;
+    }
+    if (!finite_d(g)) atomicOr(P.flag, 1);
+    if (MODE == 0)
+        out[i] = g;
+    else
+        out[i] = (g - g0[i]) * inv_eps;
+}
+
+int configure_cell_kernels(const Problem& P, int* occ)
+{
+    cudaError_t e = cudaFuncSetAttribute(k_cells<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)P.micro_smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_cells<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)P.micro_smem);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, k_cells<0>, P.micro_block, P.micro_smem);
+    if (e != cudaSuccess) {
+        set_error(std::string("configuring the cell kernel: ") + cudaGetErrorString(e));
+        return 1;
+    }
+    if (*occ < 1) *occ = 1;
+    return 0;
+}
+
+void launch_g(const Problem& P, int mode, const double* u, const double* v, const double* g0,
+              double eps, double inv_eps, double* out, cudaStream_t s)
+{
+    const int nb = (P.M.Mn + 127) / 128;
+    if (mode == 0) {
+        k_cells<0><<<P.micro_grid, P.micro_block, P.micro_smem, s>>>(P, u, v, g0, eps, inv_eps, out);
+        k_macro_nodes<0><<<nb, 128, 0, s>>>(P, u, v, g0, eps, inv_eps, out);
+    } else {
+        k_cells<1><<<P.micro_grid, P.micro_block, P.micro_smem, s>>>(P, u, v, g0, eps, inv_eps, out);
+        k_macro_nodes<1><<<nb, 128, 0, s>>>(P, u, v, g0, eps, inv_eps, out);
+    }
+}
+
+// ---- fixed-order reductions ------------------------------------------------
+// Block b covers items [8192 b, 8192 (b+1)); thread t sums items
+// 8192 b + 256 s + t (s ascending); warps combine by xor butterfly, the 8
+// warp sums as ((w0+w1)+(w2+w3))+((w4+w5)+(w6+w7)).  The last block to
+// finish reduces the block sums the same way (thread t: P[t], P[t+256], ...).
+static constexpr int kRedThreads = 256;
+static constexpr int kRedChunk = 8192;
+
+int reduction_blocks(long long n) { return (int)((n + kRedChunk - 1) / kRedChunk); }
+
+__device__ __forceinline__ double block_sum_256(double a, double* ws)
+{
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1) a = a + __shfl_xor_sync(0xffffffffu, a, d);
+    const int warp = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) ws[warp] = a;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0) r = ((ws[0] + ws[1]) + (ws[2] + ws[3])) + ((ws[4] + ws[5]) + (ws[6] + ws[7]));
+    __syncthreads();
+    return r;
+}
+
+// called by all threads with the block's partial sum (valid on thread 0)
+__device__ __forceinline__ void finish_reduction(double r, double* partials, unsigned int* counter,
+                                                 double* res)
+{
+    __shared__ double ws[8];
+    __shared__ int last;
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = r;
+        __threadfence();
+        unsigned int prev = atomicAdd(counter, 1u);
+        last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double a = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += kRedThreads) a = a + __ldcg(partials + i);
+    double tot = block_sum_256(a, ws);
+    if (threadIdx.x == 0) {
+        *res = tot;
+        *counter = 0u;
+    }
+}
+
+template <class Term>
+__global__ void __launch_bounds__(kRedThreads) k_reduce(Term term, long long n, double* partials,
+                                                        unsigned int* counter, double* res)
+{
+    __shared__ double ws[8];
+    const long long base = (long long)blockIdx.x * kRedChunk + threadIdx.x;
+    double a = 0.0;
+#pragma unroll 4
+    for (int s = 0; s < kRedChunk / kRedThreads; ++s) {
+        const long long i = base + (long long)s * kRedThreads;
+        if (i < n) a = term(i, a);
+    }
+    double r = block_sum_256(a, ws);
+    finish_reduction(r, partials, counter, res);
+}
+
+struct TermDot {
+    const double* x;
+    const double* y;
+    __device__ double operator()(long long i, double a) const { return fma(x[i], y[i], a); }
+};
+struct TermSum {
+    const double* x;
+    __device__ double operator()(long long i, double a) const { return a + x[i]; }
+};
+struct TermWsq {
+    const double* x;
+    const double* w;
+    __device__ double operator()(long long i, double a) const
+    {
+        double r = x[i] * w[i];
+        return fma(r, r, a);
+    }
+};
+struct TermMgs {
+    double* w;
+    const double* vi;
+    const double* h;
+    const double* vn;
+    __device__ double operator()(long long i, double a) const
+    {
+        double wn = fma(-(*h), vi[i], w[i]);
+        w[i] = wn;
+        return fma(wn, vn ? vn[i] : wn, a);
+    }
+};
+struct TermScaleWsq {
+    const double* w;
+    const double* ih;
+    double* v;
+    const double* winv;
+    __device__ double operator()(long long i, double a) const
+    {
+        double vv = w[i] * (*ih);
+        v[i] = vv;
+        double r = vv * winv[i];
+        return fma(r, r, a);
+    }
+};
+struct TermErr {
+    const double* g1;
+    const double* g0;
+    const double* V;
+    long long ldV;
+    const double* z;
+    int mz;
+    double dt3;
+    const double* winv;
+    __device__ double operator()(long long i, double a) const
+    {
+        double d = g1[i] - g0[i];
+        for (int q = 0; q < mz; ++q) d = fma(-z[q], V[(long long)q * ldV + i], d);
+        double e = d * dt3;
+        double r = e * winv[i];
+        return fma(r, r, a);
+    }
+};
+
+void launch_dot(const double* x, const double* y, long long n, double* res, RedWork w, cudaStream_t s)
+{
+    k_reduce<<<reduction_blocks(n), kRedThreads, 0, s>>>(TermDot{x, y}, n, w.partials, w.counter, res);
+}
+void launch_vsum(const double* x, long long n, double* res, RedWork w, cudaStream_t s)
+{
+    k_reduce<<<reduction_blocks(n), kRedThreads, 0, s>>>(TermSum{x}, n, w.partials, w.counter, res);
+}
+void launch_wsq(const double* x, const double* winv, long long n, double* res, RedWork w, cudaStream_t s)
+{
+    k_reduce<<<reduction_blocks(n), kRedThreads, 0, s>>>(TermWsq{x, winv}, n, w.partials, w.counter, res);
+}
+void launch_mgs(double* w, const double* vi, const double* h, const double* vnext, long long n,
+                double* res, RedWork rw, cudaStream_t s)
+{
+    k_reduce<<<reduction_blocks(n), kRedThreads, 0, s>>>(TermMgs{w, vi, h, vnext}, n, rw.partials,
+                                                         rw.counter, res);
+}
+
+// h = sqrt(hsq) (stored as H(j+1,j)) and its reciprocal, once
+__global__ void k_store_sqrt(const double* hsq, double* hn, double* ih)
+{
+    double h = sqrt(*hsq);
+    *hn = h;
+    *ih = 1.0 / h;
+}
+
+void launch_scale_wsq(const double* w, const double* hsq, double* hn, double* ih, double* v,
+                      const double* winv, long long n, double* res, RedWork rw, cudaStream_t s)
+{
+    k_store_sqrt<<<1, 1, 0, s>>>(hsq, hn, ih);
+    k_reduce<<<reduction_blocks(n), kRedThreads, 0, s>>>(TermScaleWsq{w, ih, v, winv}, n, rw.partials,
+                                                         rw.counter, res);
+}
+void launch_err(const double* g1, const double* g0, const double* V, long long ldV, const double* z,
+                int mz, double dt3, const double* winv, long long n, double* res, RedWork rw,
+                cudaStream_t s)
+{
+    k_reduce<<<reduction_blocks(n), kRedThreads, 0, s>>>(TermErr{g1, g0, V, ldV, z, mz, dt3, winv}, n,
+                                                         rw.partials, rw.counter, res);
+}
+
+// ---- elementwise -------------------------------------------------------------
+__global__ void k_scale(const double* __restrict__ x, double a, double* __restrict__ y, long long n)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        y[i] = x[i] * a;
+}
+__global__ void k_winv(const double* __restrict__ u, double rtol, double atol, double* __restrict__ w,
+                       long long n)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        w[i] = 1.0 / fma(rtol, fabs(u[i]), atol);
+}
+__global__ void k_combine(const double* __restrict__ u, const double* __restrict__ V, long long ldV,
+                          const double* __restrict__ c, int m, double* __restrict__ out, long long n)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        double a = u[i];
+        for (int q = 0; q < m; ++q) a = fma(c[q], V[(long long)q * ldV + i], a);
+        out[i] = a;
+    }
+}
+
+static int ew_grid(long long n)
+{
+    long long b = (n + 255) / 256;
+    return (int)(b < 152LL * 32 ? (b > 0 ? b : 1) : 152LL * 32);
+}
+
+void launch_scale(const double* x, double a, double* y, long long n, cudaStream_t s)
+{
+    k_scale<<<ew_grid(n), 256, 0, s>>>(x, a, y, n);
+}
+void launch_winv(const double* u, double rtol, double atol, double* winv, long long n, cudaStream_t s)
+{
+    k_winv<<<ew_grid(n), 256, 0, s>>>(u, rtol, atol, winv, n);
+}
+void launch_combine(const double* u, const double* V, long long ldV, const double* c, int m,
+                    double* out, long long n, cudaStream_t s)
+{
+    k_combine<<<ew_grid(n), 256, 0, s>>>(u, V, ldV, c, m, out, n);
+}
+
+// ---- total water content --------------------------------------------------
+__global__ void k_water_macro(Problem P, const double* __restrict__ u, double* __restrict__ terms)
+{
+    const MacroDev& M = P.M;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M.Mn) return;
+    double Se = vg_se(u[i], P.pA, &d_tables);
+    terms[i] = (M.epsA * M.cv[i]) * fma(P.pA.dth, Se, P.pA.thr);
+}
+
+// one warp per cell; lane l sums nodes l, l+32, ... (the fixed lane order)
+__global__ void k_water_cells(Problem P, const double* __restrict__ u, double* __restrict__ terms)
+{
+    const MacroDev& M = P.M;
+    const int lane = threadIdx.x & 31;
+    const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (k >= M.Ne) return;
+    const int nv = M.nv, Ne = M.Ne, mn = P.m.mn;
+    double al[4];
+    for (int m = 0; m < nv; ++m) {
+        double a = M.sf[(long long)(m * nv) * Ne + k] * u[M.elements[k]];
+        for (int i = 1; i < nv; ++i)
+            a = fma(M.sf[(long long)(m * nv + i) * Ne + k], u[M.elements[(long long)i * Ne + k]], a);
+        al[m] = a;
+    }
+    const double s = P.cell_scale ? P.cell_scale[k] : 1.0;
+    const double cx = M.cent[k], cy = M.cent[Ne + k];
+    const long long off = (long long)M.Mn + (long long)k * mn;
+    double p = 0.0;
+    for (int l = lane; l < mn; l += 32) {
+        double hl;
+        if (P.m.bnode[l]) {
+            double px = cx, py = cy;
+            if (M.model_type != 1) {
+                px = fma(s, P.m.vec[l], cx);
+                py = fma(s, P.m.vec[mn + l], cy);
+            }
+            hl = interp_at(nv, al, px, py);
+        } else {
+            hl = u[off + l];
+        }
+        double Se = vg_se(hl, P.pB, &d_tables);
+        p = p + fma(P.pB.dth, Se, P.pB.thr) * P.m.cv[l];
+    }
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1) p = p + __shfl_xor_sync(0xffffffffu, p, d);
+    if (lane == 0) {
+        double area = M.scv[k];
+        for (int j = 1; j < nv; ++j) area += M.scv[(long long)j * Ne + k];
+        terms[M.Mn + k] = (area * M.inv_Y) * ((s * s) * p);
+    }
+}
+
+void launch_water(const Problem& P, const double* u, double* terms, double* res, RedWork rw,
+                  cudaStream_t s)
+{
+    k_water_macro<<<(P.M.Mn + 127) / 128, 128, 0, s>>>(P, u, terms);
+    k_water_cells<<<(P.M.Ne * 32 + 127) / 128, 128, 0, s>>>(P, u, terms);
+    launch_vsum(terms, (long long)P.M.Mn + P.M.Ne, res, rw, s);
+}
+
+}  // namespace tsr

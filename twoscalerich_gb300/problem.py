@@ -1,0 +1,271 @@
+"""Problem set-up and the host-side mirror of the reference's driver.
+
+``Problem`` owns everything the reference's main() assembles before its
+time loop (src/main.cpp:32-300): the preprocessed macro and micro meshes,
+the effective-conductivity table, the two soils, ``user_data`` and the
+initial state.  ``Context`` is the GPU hot path behind the C-ABI, and
+``run_to_end`` is the reference's ``while (t < tend) exprem(...)`` loop
+(src/main.cpp:313-341).
+
+Configurations (seeded, synthetic; the reference publishes no dataset):
+  * ``config1``  -- 21x21-node triangulated macro mesh, 11x11-node square
+    inclusion per cell, Dirichlet top, N = 97,241.
+  * ``config2``  -- 201x201 macro nodes, 21x21 micro per cell with per-cell
+    inclusion size U(0.3, 0.7), Dirichlet strip x in [0.25, 0.75],
+    h0 = -5 + N(0, 0.1^2); N = 35,320,401.
+  * ``fixture10`` -- the shape of the reference's own test (10x10
+    quadrilateral macro mesh, irregular triangulated inclusion, tabulated
+    full Keff tensor, flux / free-drainage / no-flow BCs, model_type 3).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import capi, meshgen
+from .capi import check, ptr
+
+GENERATOR_SEED = 20261203
+EVAL_SEED = 7
+
+# van Genuchten materials of the configurations (m and day units)
+SOIL_A = dict(Ksat=0.054, thetar=0.03, thetas=0.37, alpha=2.8, n=2.24)
+SOIL_B = dict(Ksat=0.001, thetar=0.10, thetas=0.45, alpha=0.5, n=1.40)
+
+
+def make_soil(Ksat, thetar, thetas, alpha, n):
+    s = capi.Soil()
+    s.Ksat, s.thetar, s.thetas, s.alpha, s.n = Ksat, thetar, thetas, alpha, n
+    s.m = 1.0 - 1.0 / n                      # as src/main.cpp:127,140
+    return s
+
+
+def default_options(**kw):
+    lib = capi.load()
+    o = capi.ExpremOptions()
+    check(lib.tsr_set_exprem_options(C.byref(o)), "tsr_set_exprem_options")
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+class Problem:
+    """Preprocessed two-scale problem (host memory)."""
+
+    def __init__(self, macro, micro, keff_rows, epsA, soilA, soilB, *, macro_bc,
+                 model_type=3, boundary_flux=0.0, dirichlet_h=0.0, specific_storage=1e-6,
+                 kface=0, cell_scale=None, logh_first=None, logr=None, name=""):
+        lib = capi.load()
+        self.name = name
+        self.macro = capi.MacroMesh()
+        self.micro = capi.MicroMesh()
+        self._bc = np.ascontiguousarray(macro_bc, dtype=np.int32)
+        check(lib.tsr_macro_mesh_build(macro.nv, macro.n_nodes, ptr(macro.xy), macro.n_elems,
+                                       ptr(macro.elems), macro.bedges.size // 3, ptr(macro.bedges),
+                                       ptr(self._bc), C.byref(self.macro)), "tsr_macro_mesh_build")
+        check(lib.tsr_micro_mesh_build(micro.cell[0], micro.cell[1], micro.nv, micro.n_nodes,
+                                       ptr(micro.xy), micro.n_elems, ptr(micro.elems),
+                                       micro.bedges.size // 3, ptr(micro.bedges),
+                                       C.byref(self.micro)), "tsr_micro_mesh_build")
+        rows = np.asarray(keff_rows, dtype=np.float64)       # (n, 5): log10|h|, K11, K12, K21, K22
+        self._logh = np.ascontiguousarray(rows[:, 0])
+        self._kv = np.ascontiguousarray(rows[:, 1:].T.ravel())   # component-major
+        self.keff = capi.Keff()
+        self.keff.epsilonA = epsA
+        self.keff.no_hvalues = len(rows)
+        self.keff.logh_first = rows[0, 0] if logh_first is None else logh_first
+        self.keff.logr = (rows[1, 0] - rows[0, 0]) if logr is None else logr
+        self.keff.logh_values = ptr(self._logh)
+        self.keff.Keff_values = ptr(self._kv)
+        self.soilA = make_soil(**soilA) if isinstance(soilA, dict) else soilA
+        self.soilB = make_soil(**soilB) if isinstance(soilB, dict) else soilB
+        self.ud = capi.UserData()
+        self.ud.macro_mesh = self.macro
+        self.ud.micro_mesh = self.micro
+        self.ud.effective_conductivity = self.keff
+        self.ud.soilA = self.soilA
+        self.ud.soilB = self.soilB
+        self.ud.boundary_flux = boundary_flux
+        self.ud.model_type = model_type
+        self.ud.NUM_THREADS = 1
+        self.Mn = self.macro.no_nodes
+        self.Ne = self.macro.no_elements
+        self.mn = self.micro.no_nodes
+        self.N = self.Mn + self.Ne * self.mn
+        self.ud.N = self.N
+        self._scale = None if cell_scale is None else np.ascontiguousarray(cell_scale, np.float64)
+        self.ext = capi.ModelExt()
+        self.ext.dirichlet_h = dirichlet_h
+        self.ext.specific_storage = specific_storage
+        self.ext.kface_mode = kface
+        self.ext.cell_scale = ptr(self._scale)
+        self.dirichlet_h = dirichlet_h
+        bce = capi.as_array(self.macro.boundary_condition_edges, macro.nv * self.Ne, np.int32)
+        el = capi.as_array(self.macro.elements, macro.nv * self.Ne, np.int32)
+        nv, Ne = macro.nv, self.Ne
+        mask = np.zeros(self.Mn, bool)
+        for j in range(nv):
+            d = bce[j * Ne:(j + 1) * Ne] == 5
+            mask[el[j * Ne:(j + 1) * Ne][d]] = True
+            mask[el[((j + 1) % nv) * Ne:((j + 1) % nv + 1) * Ne][d]] = True
+        self.dirichlet_nodes = mask
+        self.options = default_options()
+        self.tspan = np.array([0.0])
+        self.tend = 1.0
+
+    def initial_state(self, h0=-5.0, noise=0.0, seed=EVAL_SEED):
+        u = np.full(self.N, h0, dtype=np.float64)
+        if noise > 0.0:
+            u += np.random.default_rng(seed).normal(0.0, noise, self.N)
+        u[:self.Mn][self.dirichlet_nodes] = self.dirichlet_h
+        return u
+
+    def array(self, name, n, dtype=np.float64, micro=False):
+        s = self.micro if micro else self.macro
+        return capi.as_array(getattr(s, name), n, dtype)
+
+    def close(self):
+        lib = capi.load()
+        if self.macro.elements:
+            lib.tsr_macro_mesh_free(C.byref(self.macro))
+        if self.micro.elements:
+            lib.tsr_micro_mesh_free(C.byref(self.micro))
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def constant_keff_rows(k=0.02):
+    """A two-row table (log10|h| = 2 and -2) holding an isotropic constant."""
+    return [[2.0, k, 0.0, 0.0, k], [-2.0, k, 0.0, 0.0, k]]
+
+
+def config1(kface=0):
+    """21x21 macro nodes (800 triangles), 11x11-node square inclusion of side
+    0.5 per cell, cell = macro spacing 0.05 m; Dirichlet h = -0.1 on the top
+    side, no flow elsewhere; h0 = -5; EXPREM tol 1e-6, Krylov <= 30,
+    t_end = 1 day, 10 saved times."""
+    macro = meshgen.macro_unit_square(21)
+    micro = meshgen.micro_square_inclusion(11, cell=0.05, side=0.5)
+    p = Problem(macro, micro, constant_keff_rows(0.02), 0.75, SOIL_A, SOIL_B,
+                macro_bc=[5, 2, 2, 2, 2], model_type=3, dirichlet_h=-0.1, kface=kface,
+                name="config1")
+    p.options = default_options(AbsTol=1e-6, RelTol=1e-6, MaxKrylov=30)
+    p.tend = 1.0
+    p.tspan = np.concatenate([[10.0], np.linspace(0.1, 1.0, 10)])
+    p.u0 = p.initial_state(-5.0)
+    return p
+
+
+def config2(n_macro=201, n_micro=21, seed=GENERATOR_SEED, eval_seed=EVAL_SEED):
+    """GPU-scale plain method: n_macro^2 macro nodes, n_micro^2 micro nodes
+    per cell, inclusion side per cell U(0.3, 0.7) of the cell (a per-cell
+    scale of the side-0.5 template), Dirichlet h = -0.1 on the top strip
+    x in [0.25, 0.75], no flow elsewhere, h0 = -5 + N(0, 0.1^2) per unknown;
+    EXPREM tol 1e-6, Krylov <= 40, t_end = 2 days."""
+    h = 1.0 / (n_macro - 1)
+    macro = meshgen.macro_unit_square(n_macro, segment=(0.25, 0.75))
+    micro = meshgen.micro_square_inclusion(n_micro, cell=h, side=0.5)
+    Ne = 2 * (n_macro - 1) ** 2
+    side = np.random.default_rng(seed).uniform(0.3, 0.7, Ne)
+    scale = side / 0.5
+    epsA = 1.0 - (0.7 ** 3 - 0.3 ** 3) / (3 * 0.4)           # 1 - E[side^2]
+    p = Problem(macro, micro, constant_keff_rows(0.02), epsA, SOIL_A, SOIL_B,
+                macro_bc=[5, 2, 2, 2, 2], model_type=3, dirichlet_h=-0.1, cell_scale=scale,
+                name="config2_%d_%d" % (n_macro, n_micro))
+    p.options = default_options(AbsTol=1e-6, RelTol=1e-6, MaxKrylov=40)
+    p.tend = 2.0
+    p.tspan = np.concatenate([[10.0], np.linspace(0.2, 2.0, 10)])
+    p.u0 = p.initial_state(-5.0, noise=0.1, seed=eval_seed)
+    return p
+
+
+def fixture10(boundary_flux=0.05, jitter=0.25, seed=GENERATOR_SEED):
+    """The shape of the reference's test scenario: 10x10 quadrilaterals,
+    influx segment x in [0, 0.4] on the top (BC 1), free drainage dh/dx = 0
+    on the south side (BC 3), no flow elsewhere (src/main.cpp:180-184),
+    model_type 3, a full 2x2 Keff(h) table, and an irregularly triangulated
+    inclusion of 11x11 nodes in a 0.1 m cell."""
+    macro = meshgen.macro_unit_square(11, quads=True, segment=(0.0, 0.4))
+    micro = meshgen.micro_square_inclusion(11, cell=0.1, side=0.6, jitter=jitter, seed=seed)
+    logh = 1.3 - 0.0333 * np.arange(100)
+    hh = 10.0 ** logh
+    k11 = 0.02 / (1.0 + (0.6 * hh) ** 2.0)
+    rows = np.stack([logh, k11, -0.06 * k11, -0.06 * k11, 0.87 * k11], 1)
+    p = Problem(macro, micro, rows, 0.64, SOIL_A, SOIL_B, macro_bc=[1, 3, 2, 2, 2],
+                model_type=3, boundary_flux=boundary_flux, name="fixture10")
+    p.options = default_options(AbsTol=1e-6, RelTol=1e-6, MaxKrylov=30)
+    p.tend = 0.5
+    p.tspan = np.concatenate([[5.0], np.linspace(0.1, 0.5, 5)])
+    p.u0 = p.initial_state(-5.0)
+    return p
+
+
+class Context:
+    """The GPU hot path of one problem (a tsr_ctx)."""
+
+    def __init__(self, problem, max_krylov=None, stream=None):
+        self.lib = capi.load()
+        self.p = problem
+        mk = problem.options.MaxKrylov if max_krylov is None else max_krylov
+        h = self.lib.tsr_init(C.byref(problem.ud), C.byref(problem.ext), stream, mk)
+        if not h:
+            raise capi.TsrError(1, "tsr_init")
+        self.h = h
+        self.N = problem.N
+
+    def g(self, u):
+        out = np.empty(self.N)
+        check(self.lib.tsr_g_eval(self.h, ptr(u), ptr(out)), "tsr_g_eval")
+        return out
+
+    def jv(self, u, g0, v, eps):
+        out = np.empty(self.N)
+        check(self.lib.tsr_jv(self.h, ptr(u), ptr(g0), ptr(v), eps, ptr(out)), "tsr_jv")
+        return out
+
+    def water(self, u):
+        w = C.c_double()
+        check(self.lib.tsr_water_content(self.h, ptr(u), C.byref(w)), "tsr_water_content")
+        return w.value
+
+    def dot(self, x, y):
+        r = C.c_double()
+        check(self.lib.tsr_dot(self.h, ptr(x), ptr(y), x.size, C.byref(r)), "tsr_dot")
+        return r.value
+
+    def exprem_step(self, t, u, tspan, solns, opts, stats):
+        tt = C.c_double(t)
+        check(self.lib.tsr_exprem_step(self.h, C.byref(tt), self.p.tend, ptr(tspan), ptr(solns),
+                                       ptr(u), C.byref(opts), C.byref(stats)), "tsr_exprem_step")
+        return tt.value
+
+    def close(self):
+        if self.h:
+            self.lib.tsr_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def run_to_end(step, problem, u0=None, max_steps=100000):
+    """The reference driver loop (src/main.cpp:311-341): call one-step
+    `step(t, u, tspan, solns, opts, stats) -> t` until t >= tend.  Returns
+    (u, tspan_solns, stats, step log)."""
+    u = (problem.u0 if u0 is None else u0).copy()
+    ns = int(problem.tspan[0])
+    solns = np.zeros((ns + 1) * problem.N)
+    solns[:problem.N] = u
+    stats = capi.ExpremStats()
+    t = 0.0
+    log = []
+    while t < problem.tend and len(log) < max_steps:
+        t = step(t, u, problem.tspan, solns, problem.options, stats)
+        log.append((stats.NumSteps, t, stats.CurrentStep, stats.CurrentKryDim))
+    return u, solns.reshape(ns + 1, problem.N), stats, log
