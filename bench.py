@@ -1,0 +1,380 @@
+#!/usr/bin/env python
+"""Benchmark of the two-scale Richards hot path on GB300.
+
+Workload (default): the GPU-scale plain method -- 201 x 201 macro nodes
+(80,000 triangles), a 21 x 21-node micro mesh per cell with per-cell
+inclusion size U(0.3, 0.7), N = 35,320,401 FP64 unknowns, EXPREM with
+tol 1e-6 and Krylov dimension <= 40 (seeded synthetic inputs; the reference
+publishes no dataset).
+
+A step is one accepted EXPREM step (the unit of the reference's driver loop,
+src/main.cpp:313-341): a G evaluation at the new state, m finite-difference
+Jacobian-vector products, modified Gram-Schmidt, phi_1(dt H_m) on the host
+and the update.  The metric is the reference's own instrument -- right-hand-
+side evaluations per second (FuncEvals / runtime, src/main.cpp:350-351) --
+over the timed steps.
+
+  value  device-resident stepping (u, G(u) and the Krylov basis in HBM);
+  e2e    the reference-facing call exprem(...) with u0 in (pinned) host
+         memory, copied in and out on every step (tsr_exprem_step).
+
+--impl reference times the CPU implementation of the same path on the host
+cores: the oracle's OpenMP form of Gfunc_parallel over the same problem (the
+reference's own Gfunc_parallel source is not in its tree).
+
+Run: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORLD = int(os.environ.get("WORLD_SIZE", "1"))
+RANK = int(os.environ.get("RANK", "0"))
+LOCAL_RANK = int(os.environ.get("LOCAL_RANK", "0"))
+if WORLD > 1:
+    # one GPU per rank: the library's CUDA runtime sees only this rank's GPU
+    os.environ["CUDA_VISIBLE_DEVICES"] = str(LOCAL_RANK)
+
+import ctypes as C  # noqa: E402
+
+import numpy as np  # noqa: E402
+
+METRIC = "G-evals/s (EXPREM FuncEvals per second)"
+UNIT = "G-evals/s"
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        if not self.proc:
+            return out
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            if vis is not None and vis.isdigit() and f[0] != vis:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if sm:
+            out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                   "reasons": sorted(reasons), "samples": len(sm)}
+        return out
+
+
+def dist_init():
+    if WORLD == 1:
+        return None
+    import torch.distributed as dist
+    dist.init_process_group("gloo")
+    return dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def allmax(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allsum(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def make_problem(args):
+    from twoscalerich_gb300 import problem as P
+    p = P.config2(n_macro=args.n_macro, n_micro=args.n_micro)
+    p.options.MaxKrylov = args.max_krylov
+    return p
+
+
+def workload(args, N):
+    return {"workload": "two-scale Richards, plain method, EXPREM steps",
+            "macro_nodes": "%dx%d" % (args.n_macro, args.n_macro),
+            "micro_nodes_per_cell": "%dx%d" % (args.n_micro, args.n_micro),
+            "cells": 2 * (args.n_macro - 1) ** 2, "unknowns": N, "max_krylov": args.max_krylov,
+            "tol": 1e-6, "inputs_vs_l2": "inputs larger than L2 (N x 8 B = %.0f MB > 129 MB)"
+            % (N * 8 / 1e6), "parallelism": "replicas" if WORLD > 1 else "1 GPU"}
+
+
+def cpu_oracle_rate(p, n_evals, threads):
+    """G evaluations per second of the oracle's OpenMP Gfunc_parallel form."""
+    import oracle
+    o = oracle.Oracle(p, nthreads=threads)
+    g = np.empty(p.N)
+    o.lib.oracle_g(o.h, o._p(p.u0), o._p(g), threads)       # first-touch / warm-up
+    t0 = time.perf_counter()
+    for _ in range(n_evals):
+        o.lib.oracle_g(o.h, o._p(p.u0), o._p(g), threads)
+    el = time.perf_counter() - t0
+    o.close()
+    return n_evals / el, el
+
+
+def run_reference(args):
+    """CPU arm: the oracle's Gfunc_parallel form on all host cores."""
+    if RANK != 0:
+        return
+    p = make_problem(args)
+    threads = os.cpu_count() or 1
+    import oracle
+    o = oracle.Oracle(p, nthreads=threads)
+    g = np.empty(p.N)
+    for _ in range(args.warmup):
+        o.lib.oracle_g(o.h, o._p(p.u0), o._p(g), threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        o.lib.oracle_g(o.h, o._p(p.u0), o._p(g), threads)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload(args, p.N),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "%d G evaluations of the full workload (one per step)"
+                                   % args.steps},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    from twoscalerich_gb300 import capi
+    from twoscalerich_gb300 import problem as P
+    dist = dist_init()
+    lib = capi.load()
+    p = make_problem(args)
+    N = p.N
+    ctx = P.Context(p, max_krylov=p.options.MaxKrylov)
+    h = ctx.h
+    fp64_peak = C.c_double()
+    capi.check(lib.tsr_fp64_peak(C.byref(fp64_peak)), "tsr_fp64_peak")
+    opts = p.options
+    st = capi.ExpremStats()
+    ns = int(p.tspan[0])
+    solns = np.zeros(1)   # the timed steps stay before the first saved time
+    tspan = p.tspan.copy()
+    tspan[0] = 0.0        # no dense output inside the benchmark
+    capi.check(lib.tsr_exprem_load(h, capi.ptr(p.u0), 0.0), "tsr_exprem_load")
+    t = C.c_double(0.0)
+
+    def advance():
+        capi.check(lib.tsr_exprem_advance(h, p.tend, capi.ptr(tspan), capi.ptr(solns),
+                                          C.byref(opts), C.byref(st), C.byref(t)),
+                   "tsr_exprem_advance")
+
+    for _ in range(args.warmup):
+        advance()
+    ev0, steps0, krylov = st.FuncEvals, st.NumSteps, []
+    clocks = Clocks()
+    clocks.start()
+    barrier(dist)
+    capi.check(lib.tsr_sync(h), "sync")
+    capi.check(lib.tsr_profile(h, 1), "profile")
+    launches0 = lib.tsr_kernel_launches()
+    capi.check(lib.tsr_mark(h, 0), "mark")
+    for _ in range(args.steps):
+        advance()
+        krylov.append(st.CurrentKryDim)
+    capi.check(lib.tsr_mark(h, 1), "mark")
+    capi.check(lib.tsr_sync(h), "sync")
+    launches = lib.tsr_kernel_launches() - launches0
+    barrier(dist)
+    clk = clocks.stop()
+    ms = C.c_double()
+    capi.check(lib.tsr_elapsed_ms(h, 0, 1, C.byref(ms)), "elapsed")
+    evals = st.FuncEvals - ev0
+    steps = st.NumSteps - steps0
+    t_max = allmax(dist, ms.value / 1e3)
+    value = allsum(dist, evals) / t_max
+    # dominant kernel: the G / Jv evaluation (cell kernel + macro node kernel)
+    gms, gcount, gbytes = C.c_double(), C.c_longlong(), C.c_double()
+    capi.check(lib.tsr_profile_read(h, 0, C.byref(gms), C.byref(gcount), C.byref(gbytes)), "prof")
+    sms, scount, sbytes = C.c_double(), C.c_longlong(), C.c_double()
+    capi.check(lib.tsr_profile_read(h, 1, C.byref(sms), C.byref(scount), C.byref(sbytes)), "prof")
+    capi.check(lib.tsr_profile(h, 0), "profile")
+    hbm_peak, peak_src = measured_peaks()
+    g_avg_ms = gms.value / max(gcount.value, 1)
+    g_bytes = gbytes.value / max(gcount.value, 1)
+    g_gbs = g_bytes / (g_avg_ms * 1e-3) / 1e9
+    gs_gbs = sbytes.value / max(sms.value * 1e-3, 1e-30) / 1e9
+    # FP64 instructions per G from the instruction counts of the cell and
+    # macro-node kernels (ncu, per unknown) -- see the kernel profiles
+    fp64_per_unknown = FP64_OPS_PER_UNKNOWN.get((args.n_macro, args.n_micro))
+    fp64 = None
+    if fp64_per_unknown:
+        ach = fp64_per_unknown * N / (g_avg_ms * 1e-3)
+        fp64 = {"achieved": ach / 1e9, "peak": fp64_peak.value / 1e9, "unit": "Gop/s",
+                "frac": ach / fp64_peak.value, "peak_source": "measured live (DFMA chains)",
+                "ops_per_G": fp64_per_unknown * N}
+
+    # e2e: the reference-facing call with u0 in pinned host memory
+    u_host = capi.PinnedArray(N)
+    capi.check(lib.tsr_exprem_store(h, u_host.a.ctypes.data_as(capi.dp)), "store")
+    te = C.c_double(t.value)
+    st2 = capi.ExpremStats()
+    C.memmove(C.byref(st2), C.byref(st), C.sizeof(st))
+
+    def step_e2e():
+        capi.check(lib.tsr_exprem_step(h, C.byref(te), p.tend, capi.ptr(tspan), capi.ptr(solns),
+                                       u_host.a.ctypes.data_as(capi.dp), C.byref(opts),
+                                       C.byref(st2)), "tsr_exprem_step")
+
+    step_e2e()   # warm (first call after a store: the state is loaded again)
+    e0 = st2.FuncEvals
+    barrier(dist)
+    capi.check(lib.tsr_sync(h), "sync")
+    capi.check(lib.tsr_mark(h, 2), "mark")
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_e2e()
+    capi.check(lib.tsr_mark(h, 3), "mark")
+    capi.check(lib.tsr_sync(h), "sync")
+    wall_e2e = time.perf_counter() - t0
+    barrier(dist)
+    ms2 = C.c_double()
+    capi.check(lib.tsr_elapsed_ms(h, 2, 3, C.byref(ms2)), "elapsed")
+    e2e_t = allmax(dist, max(ms2.value / 1e3, wall_e2e))
+    e2e_value = allsum(dist, st2.FuncEvals - e0) / e2e_t
+    u_host.free()
+
+    cpu = None
+    if RANK == 0 and WORLD == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, el = cpu_oracle_rate(p, args.cpu_evals, threads)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "%d G evaluations of the full workload by the oracle's OpenMP "
+                         "Gfunc_parallel form (%.1f s)" % (args.cpu_evals, el)}
+    traffic = G_TRAFFIC_PER_UNKNOWN.get((args.n_macro, args.n_micro))
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": WORLD, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_max / max(args.steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded generator 20261203, evaluation seed 7)",
+        "config": workload(args, N),
+        "krylov_steps_per_s": allsum(dist, steps) / t_max,
+        "dof_evals_per_s": value * N,
+        "krylov_dims": krylov,
+        "roofline": {"bound": "hbm", "kernel": "G / Jv evaluation (k_cells + k_macro_nodes)",
+                     "achieved": g_gbs, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": g_gbs / hbm_peak, "peak_source": peak_src,
+                     "traffic": None if traffic is None else traffic * N,
+                     "algorithmic_bytes_per_launch": g_bytes, "avg_launch_ms": g_avg_ms,
+                     "launches": gcount.value},
+        "fp64_roofline": fp64,
+        "gram_schmidt": {"achieved_gbs_algorithmic": gs_gbs, "peak": hbm_peak,
+                         "frac": gs_gbs / hbm_peak, "ms_total": sms.value,
+                         "share_of_step": sms.value / max(ms.value, 1e-30)},
+        "g_share_of_step": gms.value / max(ms.value, 1e-30),
+        "clocks": clk,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * N,
+                "d2h_bytes_per_step": 8 * N},
+        "gpu_launches": int(launches),
+        "cpu_baseline": cpu,
+    }
+    if RANK == 0:
+        print(json.dumps(line))
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+# FP64 instructions (DADD + DMUL + DFMA, thread level) per unknown of one G
+# evaluation, and DRAM bytes per unknown of one G launch, from the ncu
+# captures summarised in profiles/ (scaled by the unknowns processed).
+FP64_OPS_PER_UNKNOWN = {}
+G_TRAFFIC_PER_UNKNOWN = {}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n-macro", type=int, default=201)
+    ap.add_argument("--n-micro", type=int, default=21)
+    ap.add_argument("--cpu-evals", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--max-krylov", type=int, default=40)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -15,6 +15,8 @@
 #ifndef TSR_CAPI_H
 #define TSR_CAPI_H
 
+#include <stddef.h>
+
 #include "tsr_types.h"
 
 #ifdef __cplusplus
@@ -157,6 +159,31 @@ int tsr_set_default_ext(const tsr_model_ext* ext, int max_krylov);
 
 /* Releases every implicitly created context. */
 void tsr_release_all(void);
+
+/* ---- measurement hooks (no reference counterpart) ---------------------- */
+
+/* Enable (1) or disable (0) CUDA-event timing of the kernel classes inside
+ * EXPREM steps; enabling clears earlier records.  Category 0: G and
+ * finite-difference Jv evaluations; 1: the Gram-Schmidt block of an Arnoldi
+ * step.  tsr_profile_read returns the summed device time (ms), the number
+ * of timed launches and their summed algorithmic bytes. */
+int tsr_profile(tsr_ctx* ctx, int enable);
+int tsr_profile_read(tsr_ctx* ctx, int category, double* ms, long long* count, double* bytes);
+
+/* Number of kernels the library has launched since it was loaded. */
+unsigned long long tsr_kernel_launches(void);
+
+/* Measured FP64 instruction throughput of the current device (independent
+ * DFMA chains; ~20 ms). */
+int tsr_fp64_peak(double* ops_per_s);
+
+/* CUDA events on the context stream (slots 0..15) and the time between two
+ * of them; device synchronisation; pinned host buffers for host-side I/O. */
+int   tsr_mark(tsr_ctx* ctx, int slot);
+int   tsr_elapsed_ms(tsr_ctx* ctx, int slot_a, int slot_b, double* ms);
+int   tsr_sync(tsr_ctx* ctx);
+void* tsr_pinned_alloc(size_t bytes);
+void  tsr_pinned_free(void* p);
 
 #ifdef __cplusplus
 }

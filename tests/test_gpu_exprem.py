@@ -1,0 +1,88 @@
+"""EXPREM on the GPU against the oracle's EXPREM, through the C-ABI.
+
+The benchmark spec's bound is 1e-8 relative in h and in total water content at
+every saved time.  Because G, Jv, every reduction and the host-side
+decisions follow the same operation sequence, the trajectories are in fact
+required to agree bit for bit (same steps, Krylov dimensions, FuncEvals).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle
+from twoscalerich_gb300 import capi
+from twoscalerich_gb300 import problem as P
+
+pytestmark = pytest.mark.gpu
+
+TRAJ_RTOL = 1e-8
+
+
+def _compare(p, nthreads=16, max_steps=100000):
+    ctx = P.Context(p)
+    orc = oracle.Oracle(p, nthreads=nthreads)
+    ug, sg, stg, logg = P.run_to_end(ctx.exprem_step, p, max_steps=max_steps)
+    uo, so, sto, logo = P.run_to_end(orc.exprem_step, p, max_steps=max_steps)
+    assert len(logg) == len(logo)
+    assert stg.NumSteps == sto.NumSteps and stg.FuncEvals == sto.FuncEvals
+    for k in range(sg.shape[0]):
+        a, b = sg[k], so[k]
+        assert np.max(np.abs(a - b)) <= TRAJ_RTOL * np.max(np.abs(b))
+        wa, wb = ctx.water(a), orc.water(b)
+        assert abs(wa - wb) <= TRAJ_RTOL * abs(wb)
+    assert np.array_equal(sg, so)
+    assert np.array_equal(ug, uo)
+    assert logg == logo
+    return stg, logg
+
+
+def test_trajectory_config1():
+    p = P.config1()
+    st, log = _compare(p)
+    assert log[-1][1] == p.tend
+
+
+def test_trajectory_fixture10_quads():
+    p = P.fixture10()
+    _compare(p)
+
+
+def test_trajectory_config2_small_scaled_cells():
+    p = P.config2(n_macro=21, n_micro=9)
+    p.tend = 0.2
+    p.tspan = np.concatenate([[4.0], np.linspace(0.05, 0.2, 4)])
+    _compare(p)
+
+
+def test_device_resident_stepping_matches_host_stepping():
+    p = P.config1()
+    p.tend = 0.05
+    p.tspan = np.array([1.0, 0.05])
+    ctx = P.Context(p)
+    lib = capi.load()
+    uh, sh, sth, logh = P.run_to_end(ctx.exprem_step, p)
+    ctx2 = P.Context(p)
+    capi.check(lib.tsr_exprem_load(ctx2.h, capi.ptr(p.u0), 0.0), "load")
+    st = capi.ExpremStats()
+    solns = np.zeros(2 * p.N)
+    t = C.c_double(0.0)
+    while t.value < p.tend:
+        capi.check(lib.tsr_exprem_advance(ctx2.h, p.tend, capi.ptr(p.tspan), capi.ptr(solns),
+                                          C.byref(p.options), C.byref(st), C.byref(t)), "advance")
+    u = np.empty(p.N)
+    capi.check(lib.tsr_exprem_store(ctx2.h, capi.ptr(u)), "store")
+    assert np.array_equal(u, uh)
+    assert st.FuncEvals == sth.FuncEvals
+
+
+def test_dropin_gfunc_signature_path():
+    """tsr_gfunc_gpu is what the C++ Gfunc_gpu(g, u, user_data) calls."""
+    p = P.config1()
+    lib = capi.load()
+    capi.check(lib.tsr_set_default_ext(C.byref(p.ext), 30), "ext")
+    g = np.empty(p.N)
+    u = p.u0.copy()
+    capi.check(lib.tsr_gfunc_gpu(capi.ptr(g), capi.ptr(u), C.byref(p.ud)), "gfunc")
+    assert np.array_equal(g, oracle.Oracle(p).g(u))
+    lib.tsr_release_all()

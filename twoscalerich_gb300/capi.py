@@ -127,6 +127,15 @@ _SIGNATURES = {
     "tsr_gfunc_gpu": (C.c_int, [dp, dp, C.POINTER(UserData)]),
     "tsr_set_default_ext": (C.c_int, [C.POINTER(ModelExt), C.c_int]),
     "tsr_release_all": (None, []),
+    "tsr_profile": (C.c_int, [C.c_void_p, C.c_int]),
+    "tsr_profile_read": (C.c_int, [C.c_void_p, C.c_int, dp, C.POINTER(C.c_longlong), dp]),
+    "tsr_kernel_launches": (C.c_ulonglong, []),
+    "tsr_fp64_peak": (C.c_int, [dp]),
+    "tsr_mark": (C.c_int, [C.c_void_p, C.c_int]),
+    "tsr_elapsed_ms": (C.c_int, [C.c_void_p, C.c_int, C.c_int, dp]),
+    "tsr_sync": (C.c_int, [C.c_void_p]),
+    "tsr_pinned_alloc": (C.c_void_p, [C.c_size_t]),
+    "tsr_pinned_free": (None, [C.c_void_p]),
 }
 
 _lib = None
@@ -185,3 +194,21 @@ def as_array(p, n, dtype=np.float64):
     ct = C.c_double if dtype == np.float64 else C.c_int
     buf = C.cast(p, C.POINTER(ct * n)).contents
     return np.frombuffer(buf, dtype=dtype, count=n).copy()
+
+
+class PinnedArray:
+    """A float64 numpy view of page-locked host memory (cudaMallocHost)."""
+
+    def __init__(self, n):
+        lib = load()
+        self._p = lib.tsr_pinned_alloc(8 * n)
+        if not self._p:
+            raise MemoryError("tsr_pinned_alloc(%d) failed: %s" % (8 * n, last_error()))
+        buf = (C.c_double * n).from_address(self._p)
+        self.a = np.frombuffer(buf, dtype=np.float64, count=n)
+
+    def free(self):
+        if self._p:
+            self.a = None
+            load().tsr_pinned_free(self._p)
+            self._p = None

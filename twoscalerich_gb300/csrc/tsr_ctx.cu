@@ -59,6 +59,16 @@ struct tsr_ctx {
     const double* last_u0 = nullptr;
     double last_t = -1.0;
     std::vector<double> Hm, phi;
+    // optional event timing of the kernel classes inside EXPREM steps
+    struct ProfEv {
+        cudaEvent_t a, b;
+        int cat;
+        double bytes;
+    };
+    bool prof = false;
+    std::vector<ProfEv> prof_ev;
+    size_t prof_used = 0;
+    cudaEvent_t marks[16] = {};
 };
 
 namespace {
@@ -396,6 +406,40 @@ double* scal_slot(tsr_ctx* c, int slot)
     return c->d_scal + (size_t)c->ldH * (size_t)(c->maxk > 0 ? c->maxk : 1) + slot;
 }
 
+constexpr size_t kProfMax = 16384;
+
+// open an event pair of category cat (0: G / Jv, 1: Gram-Schmidt block)
+int prof_begin(tsr_ctx* c, int cat, double bytes)
+{
+    if (!c->prof) return -1;
+    if (c->prof_used >= kProfMax) return -1;
+    if (c->prof_used == c->prof_ev.size()) {
+        tsr_ctx::ProfEv e{};
+        if (cudaEventCreate(&e.a) != cudaSuccess || cudaEventCreate(&e.b) != cudaSuccess) return -1;
+        c->prof_ev.push_back(e);
+    }
+    tsr_ctx::ProfEv& e = c->prof_ev[c->prof_used];
+    e.cat = cat;
+    e.bytes = bytes;
+    cudaEventRecord(e.a, c->stream);
+    return (int)c->prof_used++;
+}
+
+void prof_end(tsr_ctx* c, int id)
+{
+    if (id >= 0) cudaEventRecord(c->prof_ev[(size_t)id].b, c->stream);
+}
+
+// algorithmic bytes of one G (u in, g out) or one Jv (u, v, g0 in, w out)
+// plus the macro geometry each evaluation must read
+double g_bytes(const tsr_ctx* c, bool jv)
+{
+    const double nv = c->P.M.nv;
+    const double per_elem = 4 * nv + 8 * nv * nv + 16 * nv + 16 * nv + 8 * nv + 16 + 4 * nv +
+                            (c->P.cell_scale ? 8 : 0);
+    return (jv ? 32.0 : 16.0) * (double)c->N + per_elem * c->Ne + 8.0 * c->Mn;
+}
+
 }  // namespace
 
 // ---- C-ABI ----------------------------------------------------------------
@@ -442,6 +486,12 @@ extern "C" void tsr_free(tsr_ctx* c)
 {
     if (!c) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto& e : c->prof_ev) {
+        cudaEventDestroy(e.a);
+        cudaEventDestroy(e.b);
+    }
+    for (auto& e : c->marks)
+        if (e) cudaEventDestroy(e);
     for (void* p : c->allocs) cudaFree(p);
     if (c->h_scal) cudaFreeHost(c->h_scal);
     if (c->h_coef) cudaFreeHost(c->h_coef);
@@ -609,7 +659,9 @@ extern "C" int tsr_exprem_advance(tsr_ctx* c, double tend, const double* tspan, 
     double* Hd = c->d_scal;   // Hessenberg block, column j at j*ldH
     if (!c->g0_valid) {
         if ((rc = reset_flag(c))) return rc;
+        int pe = prof_begin(c, 0, g_bytes(c, false));
         launch_g(c->P, 0, c->d_u, nullptr, nullptr, 0.0, 0.0, c->d_g0, s);
+        prof_end(c, pe);
         CK(cudaGetLastError());
         st->FuncEvals++;
         int flag = 0;
@@ -639,9 +691,13 @@ extern "C" int tsr_exprem_advance(tsr_ctx* c, double tend, const double* tspan, 
         launch_scale(c->d_g0, ib, V, N, s);
         for (int j = 0; j < maxk; ++j) {
             const double* vj = V + (size_t)j * N;
+            int pe = prof_begin(c, 0, g_bytes(c, true));
             launch_g(c->P, 1, c->d_u, vj, c->d_g0, eps, 1.0 / eps, c->d_w, s);
+            prof_end(c, pe);
             st->FuncEvals++;
             double* Hc = Hd + (size_t)j * ldH;
+            // Gram-Schmidt block; algorithmic minimum 8 N (j + 3) bytes
+            pe = prof_begin(c, 1, 8.0 * (double)N * (double)(j + 3));
             launch_dot(c->d_w, V, N, Hc, c->rw, s);
             for (int i = 0; i <= j; ++i) {
                 const double* vnext = (i < j) ? V + (size_t)(i + 1) * N : nullptr;
@@ -651,6 +707,7 @@ extern "C" int tsr_exprem_advance(tsr_ctx* c, double tend, const double* tspan, 
             double* vn = V + (size_t)(j + 1) * N;
             launch_scale_wsq(c->d_w, scal_slot(c, S_HSQ), Hc + j + 1, scal_slot(c, S_IH), vn,
                              c->d_winv, N, scal_slot(c, S_SV), c->rw, s);
+            prof_end(c, pe);
             CK(cudaGetLastError());
             // column j of H and the weighted norm of v_{j+1}
             CK(cudaMemcpyAsync(c->h_scal, Hc, sizeof(double) * (size_t)(j + 2), cudaMemcpyDeviceToHost, s));
@@ -702,7 +759,9 @@ extern "C" int tsr_exprem_advance(tsr_ctx* c, double tend, const double* tspan, 
             CK(cudaMemcpyAsync(c->d_unew, c->d_u, bytes, cudaMemcpyDeviceToDevice, s));
         }
         if ((rc = reset_flag(c))) return rc;
+        int pe = prof_begin(c, 0, g_bytes(c, false));
         launch_g(c->P, 0, c->d_unew, nullptr, nullptr, 0.0, 0.0, c->d_g1, s);
+        prof_end(c, pe);
         st->FuncEvals++;
         double err = 0.0;
         int mz = 0;
@@ -864,4 +923,90 @@ extern "C" int tsr_gfunc_gpu(double* g, double* u, const user_data_struct* ud)
     tsr_ctx* c = tsr::registry_get(ud, &rc);
     if (!c) return rc;
     return tsr_g_eval(c, u, g);
+}
+
+// ---- measurement hooks ----------------------------------------------------------
+
+extern "C" int tsr_profile(tsr_ctx* c, int enable)
+{
+    if (!c) return TSR_ERR_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    c->prof = enable != 0;
+    c->prof_used = 0;
+    return TSR_OK;
+}
+
+extern "C" int tsr_profile_read(tsr_ctx* c, int cat, double* ms, long long* count, double* bytes)
+{
+    if (!c || !ms || !count || !bytes) return TSR_ERR_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    double t = 0.0, b = 0.0;
+    long long n = 0;
+    for (size_t i = 0; i < c->prof_used; ++i) {
+        const tsr_ctx::ProfEv& e = c->prof_ev[i];
+        if (e.cat != cat) continue;
+        float x = 0.f;
+        CK(cudaEventElapsedTime(&x, e.a, e.b));
+        t += x;
+        b += e.bytes;
+        ++n;
+    }
+    *ms = t;
+    *count = n;
+    *bytes = b;
+    return TSR_OK;
+}
+
+extern "C" unsigned long long tsr_kernel_launches(void) { return tsr::kernel_launches(); }
+
+extern "C" int tsr_fp64_peak(double* ops_per_s)
+{
+    if (!ops_per_s) return TSR_ERR_ARG;
+    if (tsr::measure_fp64_peak(ops_per_s)) {
+        set_error("FP64 peak probe failed");
+        return TSR_ERR_CUDA;
+    }
+    return TSR_OK;
+}
+
+extern "C" int tsr_mark(tsr_ctx* c, int slot)
+{
+    if (!c || slot < 0 || slot >= 16) return TSR_ERR_ARG;
+    if (!c->marks[slot]) CK(cudaEventCreate(&c->marks[slot]));
+    CK(cudaEventRecord(c->marks[slot], c->stream));
+    return TSR_OK;
+}
+
+extern "C" int tsr_elapsed_ms(tsr_ctx* c, int a, int b, double* ms)
+{
+    if (!c || !ms || a < 0 || b < 0 || a >= 16 || b >= 16 || !c->marks[a] || !c->marks[b])
+        return TSR_ERR_ARG;
+    CK(cudaEventSynchronize(c->marks[b]));
+    float x = 0.f;
+    CK(cudaEventElapsedTime(&x, c->marks[a], c->marks[b]));
+    *ms = x;
+    return TSR_OK;
+}
+
+extern "C" int tsr_sync(tsr_ctx* c)
+{
+    if (!c) return TSR_ERR_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaDeviceSynchronize());
+    return TSR_OK;
+}
+
+extern "C" void* tsr_pinned_alloc(size_t bytes)
+{
+    void* p = nullptr;
+    if (cudaMallocHost(&p, bytes) != cudaSuccess) {
+        set_error("cudaMallocHost failed");
+        return nullptr;
+    }
+    return p;
+}
+
+extern "C" void tsr_pinned_free(void* p)
+{
+    if (p) cudaFreeHost(p);
 }

@@ -106,6 +106,11 @@ void launch_combine(const double* u, const double* V, long long ldV, const doubl
 void launch_err(const double* g1, const double* g0, const double* V, long long ldV, const double* z,
                 int mz, double dt3, const double* winv, long long n, double* res, RedWork rw,
                 cudaStream_t s);
+// number of kernels this library has launched (host counter)
+unsigned long long kernel_launches();
+// measured FP64 instruction rate of the device (DFMA chains)
+int measure_fp64_peak(double* ops_per_s);
+
 // total water content
 void launch_water(const Problem& P, const double* u, double* terms, double* res, RedWork rw,
                   cudaStream_t s);

@@ -31,6 +31,11 @@ namespace tsr {
 
 __device__ const tsr_math_tables d_tables = TSR_MATH_TABLES_INIT;
 
+// host-side count of every kernel this library launches
+static unsigned long long g_launches = 0;
+unsigned long long kernel_launches() { return g_launches; }
+static inline void count(int n = 1) { g_launches += (unsigned long long)n; }
+
 static constexpr int kTabDoubles = (int)(sizeof(tsr_math_tables) / sizeof(double));
 
 __device__ __forceinline__ void load_tables(tsr_math_tables* s)
@@ -413,6 +418,7 @@ void launch_g(const Problem& P, int mode, const double* u, const double* v, cons
               double eps, double inv_eps, double* out, cudaStream_t s)
 {
     const int nb = (P.M.Mn + 127) / 128;
+    count(2);
     if (mode == 0) {
         k_cells<0><<<P.micro_grid, P.micro_block, P.micro_smem, s>>>(P, u, v, g0, eps, inv_eps, out);
         k_macro_nodes<0><<<nb, 128, 0, s>>>(P, u, v, g0, eps, inv_eps, out);
@@ -549,19 +555,23 @@ struct TermErr {
 
 void launch_dot(const double* x, const double* y, long long n, double* res, RedWork w, cudaStream_t s)
 {
+    count();
     k_reduce<<<reduction_blocks(n), kRedThreads, 0, s>>>(TermDot{x, y}, n, w.partials, w.counter, res);
 }
 void launch_vsum(const double* x, long long n, double* res, RedWork w, cudaStream_t s)
 {
+    count();
     k_reduce<<<reduction_blocks(n), kRedThreads, 0, s>>>(TermSum{x}, n, w.partials, w.counter, res);
 }
 void launch_wsq(const double* x, const double* winv, long long n, double* res, RedWork w, cudaStream_t s)
 {
+    count();
     k_reduce<<<reduction_blocks(n), kRedThreads, 0, s>>>(TermWsq{x, winv}, n, w.partials, w.counter, res);
 }
 void launch_mgs(double* w, const double* vi, const double* h, const double* vnext, long long n,
                 double* res, RedWork rw, cudaStream_t s)
 {
+    count();
     k_reduce<<<reduction_blocks(n), kRedThreads, 0, s>>>(TermMgs{w, vi, h, vnext}, n, rw.partials,
                                                          rw.counter, res);
 }
@@ -577,6 +587,7 @@ __global__ void k_store_sqrt(const double* hsq, double* hn, double* ih)
 void launch_scale_wsq(const double* w, const double* hsq, double* hn, double* ih, double* v,
                       const double* winv, long long n, double* res, RedWork rw, cudaStream_t s)
 {
+    count(2);
     k_store_sqrt<<<1, 1, 0, s>>>(hsq, hn, ih);
     k_reduce<<<reduction_blocks(n), kRedThreads, 0, s>>>(TermScaleWsq{w, ih, v, winv}, n, rw.partials,
                                                          rw.counter, res);
@@ -585,6 +596,7 @@ void launch_err(const double* g1, const double* g0, const double* V, long long l
                 int mz, double dt3, const double* winv, long long n, double* res, RedWork rw,
                 cudaStream_t s)
 {
+    count();
     k_reduce<<<reduction_blocks(n), kRedThreads, 0, s>>>(TermErr{g1, g0, V, ldV, z, mz, dt3, winv}, n,
                                                          rw.partials, rw.counter, res);
 }
@@ -622,15 +634,18 @@ static int ew_grid(long long n)
 
 void launch_scale(const double* x, double a, double* y, long long n, cudaStream_t s)
 {
+    count();
     k_scale<<<ew_grid(n), 256, 0, s>>>(x, a, y, n);
 }
 void launch_winv(const double* u, double rtol, double atol, double* winv, long long n, cudaStream_t s)
 {
+    count();
     k_winv<<<ew_grid(n), 256, 0, s>>>(u, rtol, atol, winv, n);
 }
 void launch_combine(const double* u, const double* V, long long ldV, const double* c, int m,
                     double* out, long long n, cudaStream_t s)
 {
+    count();
     k_combine<<<ew_grid(n), 256, 0, s>>>(u, V, ldV, c, m, out, n);
 }
 
@@ -690,9 +705,57 @@ __global__ void k_water_cells(Problem P, const double* __restrict__ u, double* _
 void launch_water(const Problem& P, const double* u, double* terms, double* res, RedWork rw,
                   cudaStream_t s)
 {
+    count(2);
     k_water_macro<<<(P.M.Mn + 127) / 128, 128, 0, s>>>(P, u, terms);
     k_water_cells<<<(P.M.Ne * 32 + 127) / 128, 128, 0, s>>>(P, u, terms);
     launch_vsum(terms, (long long)P.M.Mn + P.M.Ne, res, rw, s);
+}
+
+}  // namespace tsr
+
+namespace tsr {
+
+// FP64 pipe peak: independent DFMA chains, 8 per thread (the bound of the
+// right-hand side on GB300).  Returns FP64 instructions per second.
+__global__ void k_fp64_peak(double* out, double a, double b, int iters)
+{
+    double x0 = threadIdx.x * 1e-3, x1 = x0 + 1.0, x2 = x0 + 2.0, x3 = x0 + 3.0;
+    double x4 = x0 + 4.0, x5 = x0 + 5.0, x6 = x0 + 6.0, x7 = x0 + 7.0;
+    for (int i = 0; i < iters; ++i) {
+        x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+        x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+    double s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+    if (s == 1234.5678) out[0] = s;
+}
+
+int measure_fp64_peak(double* ops_per_s)
+{
+    int nsm = 0, dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 1;
+    double* d = nullptr;
+    if (cudaMalloc(&d, 64) != cudaSuccess) return 1;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int blocks = nsm * 8, threads = 256, iters = 4096;
+    float best = 1e30f;
+    for (int r = 0; r < 3; ++r) {
+        cudaEventRecord(e0);
+        k_fp64_peak<<<blocks, threads>>>(d, 0.999, 1e-3, iters);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (r > 0 && ms < best) best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(d);
+    if (cudaGetLastError() != cudaSuccess) return 1;
+    *ops_per_s = (double)blocks * threads * iters * 8.0 / (best * 1e-3);
+    return 0;
 }
 
 }  // namespace tsr
