@@ -1,15 +1,21 @@
 """Generate tsr_math_tables.h: the lookup tables of the table-driven FP64
-logarithm and exponential used by tsr_math.h.
+logarithm and exponential of tsr_math.h.
 
 Method: P. T. P. Tang, "Table-driven implementation of the exponential
 function in IEEE floating-point arithmetic", ACM TOMS 15(2), 1989, and
 "Table-driven implementation of the logarithm function in IEEE
-floating-point arithmetic", ACM TOMS 16(4), 1990.  The tables hold
-mathematical constants evaluated here in 200-bit arithmetic (mpmath) and
-rounded to nearest double (hi) plus the rounded remainder (lo), so the
-header is identical on every host and device that includes it.
+floating-point arithmetic", ACM TOMS 16(4), 1990 -- breakpoints c_i =
+1 + i/256 for the logarithm and 2^(j/256) for the exponential.  The entries
+are mathematical constants evaluated here in 200-bit arithmetic (mpmath)
+and stored as fixed-point integers, so the header is identical on every host
+and device that includes it:
 
-Run:  python twoscalerich_gb300/csrc/gen_math_tables.py > twoscalerich_gb300/csrc/tsr_math_tables.h
+  log:  1/c_i * 2^63 (unsigned), log(c_i) split into a multiple of 2^-42
+        (stored as the integer log(c_i) * 2^42) and the remainder * 2^69;
+  exp:  2^(j/256) * 2^62, and 2^(j/256) as a double plus its remainder
+        (used where expm1 cancels).
+
+Run:  python gen_math_tables.py > tsr_math_tables.h
 """
 import mpmath
 
@@ -18,14 +24,8 @@ BITS = 8
 N = 1 << BITS
 
 
-def hexd(x):
-    return float(x).hex()
-
-
-def split(x):
-    hi = float(x)
-    lo = float(x - mpmath.mpf(hi))
-    return hi, lo
+def rnd(x):
+    return int(mpmath.nint(x))
 
 
 def main():
@@ -36,28 +36,42 @@ def main():
     out.append("#define TSR_TBL_BITS %d" % BITS)
     out.append("#define TSR_TBL_N %d" % N)
     ln2 = mpmath.log(2)
-    h, l = split(ln2)
-    out.append("#define TSR_LN2_HI %s" % hexd(h))
-    out.append("#define TSR_LN2_LO %s" % hexd(l))
-    h, l = split(ln2 / N)
-    out.append("#define TSR_LN2_N_HI %s  /* ln2 / %d */" % (hexd(h), N))
-    out.append("#define TSR_LN2_N_LO %s" % hexd(l))
-    out.append("#define TSR_N_LN2 %s  /* %d / ln2 */" % (hexd(N / ln2), N))
-    out.append("#define TSR_INV_LN10 %s  /* 1 / ln10 */" % hexd(1 / mpmath.log(10)))
-    # log table: c_i = 1 + i/N, entries {1/c_i, log(c_i) hi, log(c_i) lo, 0}
-    out.append("/* {1/c_i, log(c_i) hi, log(c_i) lo, 0} with c_i = 1 + i/%d */" % N)
+    out.append("#define TSR_LN2_N_HI %s  /* ln2 / %d, high part */" % (float(ln2 / N).hex(), N))
+    out.append("#define TSR_LN2_N_LO %s" % float(ln2 / N - mpmath.mpf(float(ln2 / N))).hex())
+    out.append("#define TSR_N_LN2 %s  /* %d / ln2 */" % (float(N / ln2).hex(), N))
+    out.append("#define TSR_INV_LN10 %s  /* 1 / ln10 */" % float(1 / mpmath.log(10)).hex())
+    l42 = rnd(ln2 * 2 ** 42)
+    out.append("#define TSR_LN2_HI42 %dLL  /* ln2 * 2^42, rounded */" % l42)
+    out.append("#define TSR_LN2_R90 %dLL  /* (ln2 - TSR_LN2_HI42 * 2^-42) * 2^90 */"
+               % rnd((ln2 - mpmath.mpf(l42) / 2 ** 42) * 2 ** 90))
+    # fixed-point Taylor coefficients
+    for k in range(1, 9):
+        out.append("#define TSR_LOG1P_Q%d %dLL  /* (-1)^(k+1)/k * 2^62 */"
+                   % (k, rnd(mpmath.mpf((-1) ** (k + 1)) / k * 2 ** 62)))
+    for k in range(1, 8):
+        out.append("#define TSR_EXPM1_Q%d %dLL  /* 1/k! * 2^62 */"
+                   % (k, rnd(mpmath.mpf(1) / mpmath.factorial(k) * 2 ** 62)))
+    out.append("/* {2^63/c_i, log(c_i)*2^42 rounded, remainder*2^69, 0}, c_i = 1 + i/%d */" % N)
     out.append("#define TSR_LOG_TABLE_INIT { \\")
     for i in range(N):
         c = 1 + mpmath.mpf(i) / N
-        inv = float(1 / c)
-        hi, lo = split(mpmath.log(c))
-        out.append("  {%s, %s, %s, 0.0}, \\" % (hexd(inv), hexd(hi), hexd(lo)))
+        inv = rnd(2 ** 63 / c)
+        hi = rnd(mpmath.log(c) * 2 ** 42)
+        r = rnd((mpmath.log(c) - mpmath.mpf(hi) / 2 ** 42) * 2 ** 69)
+        out.append("  {%dULL, %dLL, %dLL, 0LL}, \\" % (inv, hi, r))
     out.append("}")
-    out.append("/* {2^(j/%d) hi, lo} */" % N)
+    out.append("/* 2^(j/%d) * 2^62 */" % N)
     out.append("#define TSR_EXP_TABLE_INIT { \\")
     for j in range(N):
-        hi, lo = split(mpmath.power(2, mpmath.mpf(j) / N))
-        out.append("  {%s, %s}, \\" % (hexd(hi), hexd(lo)))
+        out.append("  %dLL, \\" % rnd(mpmath.power(2, mpmath.mpf(j) / N) * 2 ** 62))
+    out.append("}")
+    out.append("/* {2^(j/%d) rounded to double, remainder rounded to double} */" % N)
+    out.append("#define TSR_EXP_DTABLE_INIT { \\")
+    for j in range(N):
+        v = mpmath.power(2, mpmath.mpf(j) / N)
+        hi = float(v)
+        lo = float(v - mpmath.mpf(hi))
+        out.append("  {%s, %s}, \\" % (hi.hex(), lo.hex()))
     out.append("}")
     out.append("#endif")
     print("\n".join(out))

@@ -1,33 +1,44 @@
 /*
- * tsr_math.h -- table-driven FP64 elementary functions shared, operation for
- * operation, by the sm_103a kernels and by every host-side evaluation of the
- * two-scale right-hand side.
+ * tsr_math.h -- FP64 elementary functions evaluated mostly on the integer
+ * pipe, shared operation for operation by the sm_103a kernels and by every
+ * host-side evaluation of the two-scale right-hand side.
  *
  * Why a private libm: the finite-difference Jacobian-vector product
  * Jv = (G(u + eps v) - G(u)) / eps divides any last-bit difference in G by
  * eps (~1e-8 relative), so two G implementations agree to 1e-12 in Jv only
  * if they agree bit for bit in G.  Bitwise agreement needs the same log/exp
- * on host and device, and the same sequence of IEEE operations around them.
- * Everything here is built from +, -, *, fma and integer bit manipulation
- * only; no host or device math library call is involved, and the code is
- * compiled without floating-point contraction on both sides.
+ * on host and device, and the same sequence of operations around them.
+ *
+ * Why the integer pipe: on GB300 the FP64 pipe retires ~1.65 instructions
+ * per clock per SM (0.50 Top/s measured) while the 32-bit integer pipe
+ * retires ~64.  The two-scale G is bound by FP64 instruction count, and its
+ * van Genuchten relations need five elementary functions per node.  Here
+ * the table look-ups, the Taylor polynomials and the final rounding to a
+ * double run as exact 64-bit fixed-point integer arithmetic (64x64 -> high
+ * 64 multiplies); the FP64 pipe is used only where a double-precision
+ * argument reduction is cheaper than its integer equivalent.  Integer
+ * arithmetic is exactly reproducible, so host and device still agree bit
+ * for bit.
  *
  * Methods (published): P. T. P. Tang, "Table-driven implementation of the
  * exponential function in IEEE floating-point arithmetic", ACM TOMS 15(2),
- * 1989 (reduction x = (k/256) ln2 + r, 2^(j/256) table, polynomial in r);
- * P. T. P. Tang, "Table-driven implementation of the logarithm function in
- * IEEE floating-point arithmetic", ACM TOMS 16(4), 1990 (breakpoints
- * c_i = 1 + i/256, log(x) = E ln2 + log(c_i) + log1p((m - c_i)/c_i)).
- * The polynomials are the Taylor series of log1p and expm1 truncated where
- * the remainder falls below 2^-58 on the reduced interval.
+ * 1989 (x = (k/256) ln2 + r, 2^(j/256) table); P. T. P. Tang, "Table-driven
+ * implementation of the logarithm function in IEEE floating-point
+ * arithmetic", ACM TOMS 16(4), 1990 (c_i = 1 + i/256, log x = E ln2 +
+ * log c_i + log1p(u), u = (m - c_i)/c_i).  The polynomials are Taylor
+ * series truncated below 2^-62 on the reduced interval; E ln2 + log c_i is
+ * split into an exact multiple of 2^-42 and a remainder carried in fixed
+ * point, so the result is rounded once.
  *
- * FP64 operation counts (the unit that bounds the kernels on GB300):
- *   tsr_log 14, tsr_log1p 18, tsr_exp 11, tsr_expm1 12.
+ * FP64 instructions per call: tsr_log 1 (2 near x = 1), tsr_log1p_s 3
+ * (0 for t < 2^-8), tsr_exp 4, tsr_expm1 1 for |x| < 2^-8, else 5 (8 for
+ * |x| < ln2/2, where the result cancels against 1).  Accuracy against
+ * glibc: within 1 ulp (tested).
  *
  * Deliberate domain limits (documented, tested):
  *   tsr_exp(x)   = 0 for x <= -707 (true value < 1e-307), inf above 709.78.
  *   tsr_expm1(x) = -1 for x <= -707.
- *   tsr_log1p(t) is meant for t >= 0 (used with t = (alpha|h|)^n).
+ *   tsr_log1p(t) is for t >= 0 (used with t = (alpha|h|)^n).
  */
 #ifndef TSR_MATH_H
 #define TSR_MATH_H
@@ -43,14 +54,15 @@
 #define TSR_HD static inline
 #endif
 
-typedef struct { double invc, logc_hi, logc_lo, pad; } tsr_log_entry;
-typedef struct { double hi, lo; } tsr_exp_entry;
+typedef struct { uint64_t invc63; int64_t logc_hi42, logc_r69, pad; } tsr_log_entry;
+typedef struct { double hi, lo; } tsr_exp_dentry;
 typedef struct {
     tsr_log_entry lg[TSR_TBL_N];
-    tsr_exp_entry ex[TSR_TBL_N];
+    int64_t ex62[TSR_TBL_N];
+    tsr_exp_dentry exd[TSR_TBL_N];
 } tsr_math_tables;
 
-#define TSR_MATH_TABLES_INIT { TSR_LOG_TABLE_INIT, TSR_EXP_TABLE_INIT }
+#define TSR_MATH_TABLES_INIT { TSR_LOG_TABLE_INIT, TSR_EXP_TABLE_INIT, TSR_EXP_DTABLE_INIT }
 
 TSR_HD uint64_t tsr_d2u(double x)
 {
@@ -74,6 +86,41 @@ TSR_HD double tsr_u2d(uint64_t u)
 #endif
 }
 
+/* high 64 bits of the 128-bit product */
+TSR_HD uint64_t tsr_umulhi(uint64_t a, uint64_t b)
+{
+#if defined(__CUDA_ARCH__)
+    return __umul64hi(a, b);
+#else
+    return (uint64_t)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+/* high 64 bits of the signed 128-bit product (floor of a*b / 2^64) */
+TSR_HD int64_t tsr_smulhi(int64_t a, int64_t b)
+{
+#if defined(__CUDA_ARCH__)
+    return __mul64hi(a, b);
+#else
+    return (int64_t)(((__int128)a * b) >> 64);
+#endif
+}
+
+TSR_HD int tsr_clz64(uint64_t x)   /* x != 0 */
+{
+#if defined(__CUDA_ARCH__)
+    return __clzll((long long)x);
+#else
+    return __builtin_clzll(x);
+#endif
+}
+
+/* floor(v / 2^n) for signed v, 0 <= n < 64 */
+TSR_HD int64_t tsr_sar(int64_t v, int n)
+{
+    return v >= 0 ? (int64_t)((uint64_t)v >> n) : (int64_t)~((~(uint64_t)v) >> n);
+}
+
 #define TSR_SHIFTER 0x1.8p52            /* 1.5 * 2^52 */
 #define TSR_SHIFTER_BITS 0x4338000000000000ull
 #define TSR_ONE_BITS 0x3FF0000000000000ull
@@ -84,51 +131,105 @@ TSR_HD double tsr_u2d(uint64_t u)
 #define TSR_EXP_FAST_LIMIT_BITS 0x4086180000000000ull  /* 707.0 */
 #define TSR_EXP_OVERFLOW 0x1.62e42fefa39efp+9          /* 709.78271289338397 */
 
-/* log(x + corr) for positive, normal, finite x, where corr is a correction
- * far below ulp(x) scale (the rounding error of x); use_corr selects it. */
-TSR_HD double tsr_log_core(double x, double corr, int use_corr,
-                           const tsr_math_tables* T)
+/* Round v * 2^-scale to the nearest double (ties to even).  The result
+ * must be a normal double; v == 0 gives +0. */
+TSR_HD double tsr_fix2d(int64_t v, int scale)
+{
+    if (v == 0) return 0.0;
+    uint64_t sgn = v < 0 ? 0x8000000000000000ull : 0ull;
+    uint64_t a = v < 0 ? (uint64_t)0 - (uint64_t)v : (uint64_t)v;
+    int msb = 63 - tsr_clz64(a);
+    uint64_t mant;
+    if (msb > 52) {
+        int sh = msb - 52;
+        uint64_t rem = a & ((1ull << sh) - 1);
+        uint64_t half = 1ull << (sh - 1);
+        mant = a >> sh;
+        if (rem > half || (rem == half && (mant & 1ull))) mant += 1;
+    } else {
+        mant = a << (52 - msb);
+    }
+    int64_t eb = (int64_t)msb - scale + 1023;       /* biased exponent */
+    return tsr_u2d(sgn | (((uint64_t)(eb - 1) << 52) + mant));
+}
+
+/* trunc(r * 2^scale) as a signed integer; |r| * 2^scale must be < 2^62 */
+TSR_HD int64_t tsr_d2fix(double r, int scale)
+{
+    uint64_t b = tsr_d2u(r);
+    int e = (int)((b >> 52) & 0x7FF);
+    if (e == 0) return 0;
+    uint64_t m = (b & TSR_MANT_MASK) | (1ull << 52);
+    int sh = e - 1075 + scale;
+    uint64_t a;
+    if (sh >= 0) a = m << sh;
+    else if (sh > -64) a = m >> (-sh);
+    else a = 0;
+    return (b >> 63) ? -(int64_t)a : (int64_t)a;
+}
+
+/* Q(u) = log1p(u)/u = 1 - u/2 + u^2/3 - ... - u^6/6 + u^7/7, |u| < 2^-8,
+ * u given at scale 2^64; result at scale 2^62 */
+TSR_HD int64_t tsr_log1p_q(int64_t U64)
+{
+    int64_t q = TSR_LOG1P_Q7;
+    q = TSR_LOG1P_Q6 + tsr_smulhi(U64, q);
+    q = TSR_LOG1P_Q5 + tsr_smulhi(U64, q);
+    q = TSR_LOG1P_Q4 + tsr_smulhi(U64, q);
+    q = TSR_LOG1P_Q3 + tsr_smulhi(U64, q);
+    q = TSR_LOG1P_Q2 + tsr_smulhi(U64, q);
+    return TSR_LOG1P_Q1 + tsr_smulhi(U64, q);
+}
+
+/* log1p(u) for an exact double u, 0 < |u| < 2^-8, with relative accuracy:
+ * the exact mantissa of u times Q(u) in integer arithmetic. */
+TSR_HD double tsr_log1p_small(double u)
+{
+    uint64_t b = tsr_d2u(u);
+    int e = (int)((b >> 52) & 0x7FF);
+    if (e == 0) return u;                               /* zero or subnormal */
+    int64_t Q = tsr_log1p_q(tsr_d2fix(u, 64));
+    uint64_t m = ((b & TSR_MANT_MASK) | (1ull << 52)) << 11;   /* leading bit 63 */
+    int64_t P = (int64_t)tsr_umulhi(m, (uint64_t)Q);    /* |u| Q at scale 2^(1084 - e) */
+    double r = tsr_fix2d(P, 1084 - e);
+    return (b >> 63) ? -r : r;
+}
+
+/* log(x + corr) for positive normal finite x away from 1 (x outside
+ * [1 - 2^-9, 1 + 2^-8)); corr is a correction of the order of the rounding
+ * error of x (use_corr selects it). */
+TSR_HD double tsr_log_core(double x, double corr, int use_corr, const tsr_math_tables* T)
 {
     uint64_t b = tsr_d2u(x);
     int64_t E = (int64_t)(b >> 52) - 1023;
-    unsigned i = (unsigned)(b >> 44) & 0xFFu;
-    uint64_t mb = (b & TSR_MANT_MASK) | TSR_ONE_BITS;                /* [1,2) */
-    /* x in [1 - 2^-9, 1): reduce against c = 1 (u = x - 1, exact) so the
-     * result keeps its relative accuracy instead of cancelling -ln2 + log c. */
-    if (b >= 0x3FEFF00000000000ull && b < TSR_ONE_BITS) {
-        E = 0;
-        i = 0;
-        mb = b;
+    uint64_t mant = b & TSR_MANT_MASK;
+    unsigned i = (unsigned)(mant >> 44);
+    const tsr_log_entry* t = &T->lg[i];
+    /* u = (m - c_i)/c_i at scale 2^71: (m - c_i) * 2^72 = low 44 bits << 20 */
+    int64_t U71 = (int64_t)tsr_umulhi((mant & 0xFFFFFFFFFFFull) << 20, t->invc63);
+    if (use_corr) {
+        /* + corr 2^-E / c_i */
+        int64_t C = tsr_d2fix(corr, (int)(71 - E));
+        U71 += tsr_smulhi(C * 2, (int64_t)(t->invc63 >> 1)) * 2;
     }
-    double m = tsr_u2d(mb);
-    double c = tsr_u2d(TSR_ONE_BITS | ((uint64_t)i << 44));         /* 1+i/256 */
-    double f = m - c;                                                /* exact */
-    if (use_corr && E < 1023)
-        f = fma(corr, tsr_u2d((uint64_t)(1023 - E) << 52), f);      /* corr*2^-E */
-    const tsr_log_entry* e = &T->lg[i];
-    double u = f * e->invc;                                          /* [0,2^-8) */
-    /* log1p(u) = u + u^2 q(u), q = -1/2 + u/3 - u^2/4 + u^3/5 - u^4/6 + u^5/7 */
-    double q = fma(u, 0x1.2492492492492p-3, -0x1.5555555555555p-3);
-    q = fma(q, u, 0x1.999999999999ap-3);
-    q = fma(q, u, -0.25);
-    q = fma(q, u, 0x1.5555555555555p-2);
-    q = fma(q, u, -0.5);
-    double p = fma(u * u, q, u);
-    double ed = tsr_u2d(TSR_SHIFTER_BITS + (uint64_t)E) - TSR_SHIFTER; /* (double)E */
-    double hi = fma(ed, TSR_LN2_HI, e->logc_hi);
-    double lo = fma(ed, TSR_LN2_LO, e->logc_lo);
-    return hi + (lo + p);
+    int64_t Q = tsr_log1p_q(tsr_sar(U71, 7));
+    int64_t P69 = tsr_smulhi(U71, Q);                  /* log1p(u) at scale 2^69 */
+    int64_t lo = P69 + t->logc_r69 + tsr_sar(E * TSR_LN2_R90, 21);
+    int64_t K = E * TSR_LN2_HI42 + t->logc_hi42;        /* exact multiple of 2^-42 */
+    return tsr_fix2d(K, 42) + tsr_fix2d(lo, 69);
 }
 
 /* Special operands of log: zero, negative, subnormal, inf, NaN. */
+TSR_HD double tsr_log(double x, const tsr_math_tables* T);
+
 TSR_HD double tsr_log_special(double x, const tsr_math_tables* T)
 {
     uint64_t b = tsr_d2u(x);
     if ((b & TSR_ABS_MASK) == 0) return -INFINITY;
     if (b >> 63) return tsr_u2d(0x7FF8000000000000ull);           /* NaN */
     if (b >= TSR_INF_BITS) return x + x;                           /* inf/NaN */
-    /* subnormal: scale by 2^54 */
-    return tsr_log_core(x * 0x1p54, 0.0, 0, T) - 54.0 * TSR_LN2_HI;
+    /* subnormal: log(x 2^54) - 54 ln2, the scaled value is normal and away from 1 */
+    return tsr_log_core(x * 0x1p54, 0.0, 0, T) - 54.0 * 0x1.62e42fefa39efp-1;
 }
 
 TSR_HD double tsr_log(double x, const tsr_math_tables* T)
@@ -136,14 +237,24 @@ TSR_HD double tsr_log(double x, const tsr_math_tables* T)
     uint64_t b = tsr_d2u(x);
     if (b - TSR_DBL_MIN_BITS >= TSR_INF_BITS - TSR_DBL_MIN_BITS)
         return tsr_log_special(x, T);
+    /* [1 - 2^-9, 1 + 2^-8): log1p of the exact x - 1 */
+    if (b >= 0x3FEFF00000000000ull && b < 0x3FF0100000000000ull) {
+        if (b == TSR_ONE_BITS) return 0.0;
+        return tsr_log1p_small(x - 1.0);
+    }
     return tsr_log_core(x, 0.0, 0, T);
 }
 
 /* log1p(t) for t >= 0 given s = 1 + t already rounded by the caller (the
- * two-scale model reuses s).  The rounding error of s is recovered exactly
- * (Fast2Sum ordered by magnitude) and folded into the reduced argument. */
+ * two-scale model reuses s).  For t >= 2^-8 the rounding error of s is
+ * recovered exactly (Fast2Sum ordered by magnitude) and folded into the
+ * reduced argument; below, log1p(t) = t Q(t) directly. */
 TSR_HD double tsr_log1p_s(double t, double s, const tsr_math_tables* T)
 {
+    if (tsr_d2u(t) < 0x3F70000000000000ull) {          /* 0 <= t < 2^-8 */
+        if (t == 0.0) return t;
+        return tsr_log1p_small(t);
+    }
     if (tsr_d2u(s) >= TSR_INF_BITS) return s + s;
     double corr = (t > 1.0) ? (1.0 - (s - t)) : (t - (s - 1.0));
     return tsr_log_core(s, corr, 1, T);
@@ -154,9 +265,10 @@ TSR_HD double tsr_log1p(double t, const tsr_math_tables* T)
     return tsr_log1p_s(t, 1.0 + t, T);
 }
 
-/* Shared reduction of exp/expm1: x = (k/256) ln2 + r, |r| <= ln2/512;
- * returns p = expm1(r) and sets j = k mod 256, M = (k - j)/256. */
-TSR_HD double tsr_exp_reduce(double x, unsigned* j, int64_t* M)
+/* Shared reduction of exp/expm1: x = (k/256) ln2 + r, |r| <= ln2/512
+ * (4 FP64 instructions); returns Q(r) = expm1(r)/r at scale 2^62 and sets
+ * r, j = k mod 256 and M = (k - j)/256. */
+TSR_HD int64_t tsr_exp_reduce(double x, double* r_out, unsigned* j, int64_t* M, int64_t* k_out)
 {
     double t = fma(x, TSR_N_LN2, TSR_SHIFTER);
     int64_t k = (int64_t)(tsr_d2u(t) - TSR_SHIFTER_BITS);
@@ -165,22 +277,30 @@ TSR_HD double tsr_exp_reduce(double x, unsigned* j, int64_t* M)
     r = fma(-kd, TSR_LN2_N_LO, r);
     *j = (unsigned)k & 0xFFu;
     *M = (k - (int64_t)*j) / 256;
-    /* expm1(r) = r + r^2 (1/2 + r/6 + r^2/24 + r^3/120) */
-    double q = fma(r, 0x1.1111111111111p-7, 0x1.5555555555555p-5);
-    q = fma(q, r, 0x1.5555555555555p-3);
-    q = fma(q, r, 0.5);
-    return fma(r * r, q, r);
+    *r_out = r;
+    *k_out = k;
+    /* Q(r) = 1 + r/2 + r^2/6 + r^3/24 + r^4/120 + r^5/720 */
+    int64_t R = tsr_d2fix(r, 64);
+    int64_t q = TSR_EXPM1_Q6;
+    q = TSR_EXPM1_Q5 + tsr_smulhi(R, q);
+    q = TSR_EXPM1_Q4 + tsr_smulhi(R, q);
+    q = TSR_EXPM1_Q3 + tsr_smulhi(R, q);
+    q = TSR_EXPM1_Q2 + tsr_smulhi(R, q);
+    q = TSR_EXPM1_Q1 + tsr_smulhi(R, q);
+    return q;
 }
 
-/* exp(x) for |x| < 707 (no operand checks). */
+/* exp(x) for |x| < 707 (no operand checks) */
 TSR_HD double tsr_exp_fast(double x, const tsr_math_tables* T)
 {
+    double r;
     unsigned j;
-    int64_t M;
-    double p = tsr_exp_reduce(x, &j, &M);
-    const tsr_exp_entry* e = &T->ex[j];
-    double y = e->hi + fma(e->hi, p, e->lo);
-    return tsr_u2d(tsr_d2u(y) + ((uint64_t)M << 52));
+    int64_t M, k;
+    int64_t q = tsr_exp_reduce(x, &r, &j, &M, &k);
+    int64_t p = tsr_smulhi(tsr_d2fix(r, 66), q);        /* expm1(r) at scale 2^64 */
+    int64_t Tj = T->ex62[j];
+    int64_t y = Tj + tsr_smulhi(Tj, p);                 /* 2^(j/256) e^r at scale 2^62 */
+    return tsr_fix2d(y, (int)(62 - M));
 }
 
 TSR_HD double tsr_exp_special(double x, const tsr_math_tables* T)
@@ -208,14 +328,36 @@ TSR_HD double tsr_expm1(double x, const tsr_math_tables* T)
         if (x > 0.0) return tsr_exp_special(x, T);
         return -1.0;
     }
+    if ((tsr_d2u(x) & TSR_ABS_MASK) < 0x3F70000000000000ull) {
+        /* |x| < 2^-8: expm1(x) = x Q(x) without reduction */
+        if (x == 0.0) return x;
+        int64_t R = tsr_d2fix(x, 64);
+        int64_t q = TSR_EXPM1_Q7;
+        q = TSR_EXPM1_Q6 + tsr_smulhi(R, q);
+        q = TSR_EXPM1_Q5 + tsr_smulhi(R, q);
+        q = TSR_EXPM1_Q4 + tsr_smulhi(R, q);
+        q = TSR_EXPM1_Q3 + tsr_smulhi(R, q);
+        q = TSR_EXPM1_Q2 + tsr_smulhi(R, q);
+        q = TSR_EXPM1_Q1 + tsr_smulhi(R, q);
+        return x * tsr_fix2d(q, 62);
+    }
+    double r;
     unsigned j;
-    int64_t M;
-    double p = tsr_exp_reduce(x, &j, &M);
-    const tsr_exp_entry* e = &T->ex[j];
-    double s2 = tsr_u2d((uint64_t)(1023 + M) << 52);               /* 2^M */
-    double a = e->hi * s2 - 1.0;
-    double b = fma(e->hi, p, e->lo) * s2;
-    return a + b;
+    int64_t M, k;
+    int64_t q = tsr_exp_reduce(x, &r, &j, &M, &k);
+    int64_t p = tsr_smulhi(tsr_d2fix(r, 66), q);        /* expm1(r) at scale 2^64 */
+    if (M == 0 || M == -1) {
+        /* the result cancels against 1: (T_hi 2^M - 1) is exact, the rest
+         * T_hi p + T_lo is added in double precision */
+        const tsr_exp_dentry* d = &T->exd[j];
+        double s2 = M == 0 ? 1.0 : 0.5;
+        double a = d->hi * s2 - 1.0;
+        double b = fma(d->hi, tsr_fix2d(p, 64), d->lo) * s2;
+        return a + b;
+    }
+    int64_t Tj = T->ex62[j];
+    int64_t y = Tj + tsr_smulhi(Tj, p);                 /* scale 2^62 */
+    return tsr_fix2d(y, (int)(62 - M)) - 1.0;
 }
 
 #endif /* TSR_MATH_H */
