@@ -167,7 +167,7 @@ def workload(args, N):
 def cpu_oracle_rate(p, n_evals, threads):
     """G evaluations per second of the oracle's OpenMP Gfunc_parallel form."""
     import oracle
-    o = oracle.Oracle(p, nthreads=threads)
+    o = oracle.Oracle(p, nthreads=threads, libm=True)
     g = np.empty(p.N)
     o.lib.oracle_g(o.h, o._p(p.u0), o._p(g), threads)       # first-touch / warm-up
     t0 = time.perf_counter()
@@ -185,7 +185,7 @@ def run_reference(args):
     p = make_problem(args)
     threads = os.cpu_count() or 1
     import oracle
-    o = oracle.Oracle(p, nthreads=threads)
+    o = oracle.Oracle(p, nthreads=threads, libm=True)
     g = np.empty(p.N)
     for _ in range(args.warmup):
         o.lib.oracle_g(o.h, o._p(p.u0), o._p(g), threads)
@@ -203,7 +203,8 @@ def run_reference(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload(args, p.N),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "%d G evaluations of the full workload (one per step)"
+                         "sample": "%d G evaluations of the full workload (one per step), "
+                                   "OpenMP Gfunc_parallel form with C-library log/exp"
                                    % args.steps},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -316,7 +317,8 @@ def run_ours(args):
         rate, el = cpu_oracle_rate(p, args.cpu_evals, threads)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": "%d G evaluations of the full workload by the oracle's OpenMP "
-                         "Gfunc_parallel form (%.1f s)" % (args.cpu_evals, el)}
+                         "Gfunc_parallel form with C-library log/exp (%.1f s)"
+                         % (args.cpu_evals, el)}
     traffic = G_TRAFFIC_PER_UNKNOWN.get((args.n_macro, args.n_micro))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": WORLD, "steps": args.steps,

@@ -12,9 +12,12 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(HERE, "libtsr_oracle.so")
+# same source built with the C library's log/exp (used to time the CPU baseline)
+ORACLE_LIBM_LIB = os.path.join(HERE, "libtsr_oracle_libm.so")
 REF_LIB = os.path.join(HERE, "_ref", "libtsr_ref.so")
 
 _o = None
+_om = None
 _r = None
 
 
@@ -24,13 +27,15 @@ def _sig(lib, name, res, args):
     f.argtypes = args
 
 
-def load():
-    global _o
-    if _o is None:
+def load(libm=False):
+    """The bitwise oracle, or (libm=True) its C-library-math build."""
+    global _o, _om
+    if (_om if libm else _o) is None:
         from twoscalerich_gb300 import capi
-        if not os.path.exists(ORACLE_LIB):
+        path = ORACLE_LIBM_LIB if libm else ORACLE_LIB
+        if not os.path.exists(path):
             raise OSError("oracle not built (make -C oracle oracle)")
-        lib = C.CDLL(ORACLE_LIB)
+        lib = C.CDLL(path)
         dp, vp = capi.dp, C.c_void_p
         _sig(lib, "oracle_create", vp, [C.POINTER(capi.UserData), C.POINTER(capi.ModelExt)])
         _sig(lib, "oracle_destroy", None, [vp])
@@ -50,8 +55,11 @@ def load():
         _sig(lib, "oracle_vg", None, [C.POINTER(capi.Soil), C.c_double, C.c_double, dp])
         _sig(lib, "oracle_keff", None, [C.POINTER(capi.Keff), C.c_double, dp])
         _sig(lib, "oracle_dirichlet_mask", C.c_int, [vp, C.POINTER(C.c_ubyte)])
-        _o = lib
-    return _o
+        if libm:
+            _om = lib
+        else:
+            _o = lib
+    return _om if libm else _o
 
 
 def load_ref():
@@ -76,8 +84,8 @@ def load_ref():
 class Oracle:
     """The oracle bound to one problem (twoscalerich_gb300.problem.Problem)."""
 
-    def __init__(self, problem, nthreads=1):
-        self.lib = load()
+    def __init__(self, problem, nthreads=1, libm=False):
+        self.lib = load(libm)
         self.p = problem
         self.h = self.lib.oracle_create(C.byref(problem.ud), C.byref(problem.ext))
         if not self.h:

@@ -52,6 +52,17 @@
 
 static const tsr_math_tables T = TSR_MATH_TABLES_INIT;
 
+#ifdef TSR_ORACLE_LIBM
+/* CPU-native variant used only to time the CPU baseline: the same
+ * algorithm with the host C library's log/exp/log1p/expm1 (what a CPU
+ * implementation of Gfunc_parallel would call); its results differ from the
+ * bitwise oracle in the last bits. */
+#define tsr_log(x, t) log(x)
+#define tsr_exp(x, t) exp(x)
+#define tsr_expm1(x, t) expm1(x)
+#define tsr_log1p_s(x, s, t) log1p(x)
+#endif
+
 /* ------------------------------------------------------------------ */
 /* Van Genuchten-Mualem relations (parameters include/soil.h:1-7; m = 1-1/n
  * as set at src/main.cpp:127,140).  For h < 0, with a = alpha|h|,

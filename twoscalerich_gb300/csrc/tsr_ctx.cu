@@ -11,6 +11,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -315,8 +316,13 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
     if ((rc = dev_alloc(c, sizeof(int) * 4, &p))) return rc;
     P.flag = (int*)p;
     CK(cudaMemset(P.flag, 0, sizeof(int) * 4));
-    // launch shape of the cell kernel
-    P.micro_block = 128;
+    // launch shape of the cell kernel (TSR_CELL_THREADS overrides: 64..256);
+    // 256 threads keep 32 warps per SM in flight at 4 cells per SM
+    P.micro_block = 256;
+    if (const char* e = std::getenv("TSR_CELL_THREADS")) {
+        int v = std::atoi(e);
+        if (v >= 64 && v <= 256 && v % 32 == 0) P.micro_block = v;
+    }
     const size_t tab = sizeof(tsr_math_tables);
     P.micro_smem = tab + sizeof(double) * (4 * (size_t)mn + 3 * (size_t)mNe + (size_t)T.nb + 16);
     int dev_smem = 0, nsm = 0;

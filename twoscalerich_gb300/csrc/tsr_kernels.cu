@@ -222,7 +222,7 @@ __device__ __forceinline__ void macro_element_terms(const Problem& P, int k, con
 // Dynamic shared memory: tables | h[mn] | Kh[mn] | Cd[mn] | den[mn] |
 // F[3 mNe] | items[nb] | misc[16] (interpolant coefficients, vertex heads).
 template <int MODE>
-__global__ void __launch_bounds__(128) k_cells(Problem P, const double* __restrict__ u,
+__global__ void __launch_bounds__(256) k_cells(Problem P, const double* __restrict__ u,
                                                const double* __restrict__ v,
                                                const double* __restrict__ g0, double eps,
                                                double inv_eps, double* __restrict__ out)
