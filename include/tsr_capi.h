@@ -185,6 +185,22 @@ int   tsr_sync(tsr_ctx* ctx);
 void* tsr_pinned_alloc(size_t bytes);
 void  tsr_pinned_free(void* p);
 
+/* ---- allocation-free variant (no counterpart in the reference) ---------- */
+
+/* *d_out = sum_i d_x[i] * d_y[i] over n doubles, in the same fixed order as
+ * tsr_dot (identical bits), without a context and without allocating device
+ * memory: for callers that cannot call cudaMalloc (an embedding program that
+ * owns all device memory, code running under stream capture, loops that
+ * cannot afford an allocation's synchronisation).  All pointers are device
+ * pointers; the call is asynchronous on `stream` (NULL: the default stream).
+ * Its scratch is a fixed file-scope device array of 64 KB + 256 B that every
+ * GPU loading the library keeps until exit, so n is limited to 67,108,864
+ * (larger n returns TSR_ERR_ARG).  The first call on a device looks up the
+ * array's device address; make it before any stream capture.  Calls share
+ * the array: calls that overlap on the GPU race, so serialise them. */
+int tsr_dot_device_noalloc(const double* d_x, const double* d_y, long long n,
+                           double* d_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

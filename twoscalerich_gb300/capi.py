@@ -136,6 +136,8 @@ _SIGNATURES = {
     "tsr_sync": (C.c_int, [C.c_void_p]),
     "tsr_pinned_alloc": (C.c_void_p, [C.c_size_t]),
     "tsr_pinned_free": (None, [C.c_void_p]),
+    "tsr_dot_device_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p,
+                                         C.c_void_p]),
 }
 
 _lib = None
