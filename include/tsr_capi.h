@@ -79,6 +79,13 @@ void tsr_macro_mesh_free(macro_mesh_struct* mesh);
 void tsr_micro_mesh_free(micro_mesh_struct* mesh);
 void tsr_keff_free(Keff_struct* keff);
 
+/* Overwrites the micro-boundary entries of u (N doubles, host) with the
+ * macro interpolant, as src/save_solution.cpp:256-318 does before writing a
+ * solution (the cell kernels use the interpolant there and do not evolve
+ * those entries).  ext may be NULL. */
+int tsr_calibrate_micro_boundary(const user_data_struct* user_data,
+                                 const tsr_model_ext* ext, double* u);
+
 /* Replaces phipade(double*, double*, double, int, int)
  * (src/phipade.cpp:15; include/exprem.h:28): phi_1(alpha*H(1:m,1:m)) by the
  * (6,6) Pade approximant with scaling and squaring, FP64 on the host.  H has

@@ -70,6 +70,7 @@ static const tsr_math_tables T = TSR_MATH_TABLES_INIT;
  *   K(h) = Ks Se^(1/2) (1 - (1 - Se^(1/m))^m)^2,  1 - Se^(1/m) = t/(1+t)
  *   theta(h) = theta_r + (theta_s - theta_r) Se
  *   C(h) = dtheta/dh = (theta_s-theta_r) m n t Se / (|h| (1+t))
+ *        = (theta_s-theta_r) m n Se / (|h| (1 + 1/t))
  * For h >= 0: K = Ks, theta = theta_s, C = 0.  A specific storage S_s is
  * added to C everywhere.  C is carried as the ratio Cn/Cd.                 */
 
@@ -93,7 +94,11 @@ static vgpar make_vgpar(const soil_struct* s)
     return p;
 }
 
-/* K, Cn, Cd and Se at head h */
+/* K, Cn, Cd and Se at head h.  With e = exp(-|n log(alpha|h|)|) = min(t, 1/t):
+ *   t < 1:  log(1+t) = log1p(e),          log(t/(1+t)) = nL - log1p(e)
+ *   t >= 1: log(1+t) = nL + log1p(e),     log(t/(1+t)) = -log1p(e)
+ * so no difference of nearly equal logarithms is ever formed (dry soil,
+ * t >> 1, would otherwise cancel), and t/(1+t) = e/(1+e) or 1/(1+e). */
 static void vg_eval(double h, const vgpar* p, double* K, double* Cn, double* Cd, double* Se_out)
 {
     if (h < 0.0) {
@@ -101,14 +106,17 @@ static void vg_eval(double h, const vgpar* p, double* K, double* Cn, double* Cd,
         double a = p->alpha * ah;
         double L = tsr_log(a, &T);
         double nL = p->n * L;
-        double t = tsr_exp(nL, &T);
-        double s1 = 1.0 + t;
-        double l1 = tsr_log1p_s(t, s1, &T);
+        double e = tsr_exp(-fabs(nL), &T);
+        double s1 = 1.0 + e;
+        double lp = tsr_log1p_s(e, s1, &T);
+        int dry = nL >= 0.0;
+        double l1 = dry ? nL + lp : lp;                /* log(1+t) */
+        double y = dry ? -(p->m * lp) : p->m * (nL - lp);
         double X = tsr_exp(p->mh * l1, &T);           /* Se^(1/2) */
         double Se = X * X;
-        double B = -tsr_expm1(p->m * (nL - l1), &T);   /* 1 - (t/(1+t))^m */
+        double B = -tsr_expm1(y, &T);                  /* 1 - (t/(1+t))^m */
         *K = (p->Ks * X) * (B * B);
-        *Cn = p->coefC * (t * Se);
+        *Cn = dry ? p->coefC * Se : p->coefC * (e * Se);
         *Cd = ah * s1;
         *Se_out = Se;
     } else {
@@ -469,7 +477,8 @@ static size_t scratch_doubles(const oracle_problem* P)
 
 /* g = G(x).  nthreads > 1: the micro cells run as an OpenMP loop (the
  * Gfunc_parallel form); the macro assembly is sequential in element order.
- * Returns 0 (the reference's Gfunc flag convention: 0 = success). */
+ * Returns 0, or 1 if G has a non-finite entry (the reference's Gfunc flag
+ * convention: 0 = success). */
 int oracle_g(oracle_problem* P, const double* x, double* g, int nthreads)
 {
     const macro_mesh_struct* M = &P->ud.macro_mesh;
@@ -562,6 +571,10 @@ int oracle_g(oracle_problem* P, const double* x, double* g, int nthreads)
     }
     free(acc);
     free(Q);
+    /* failure flag of the reference's Gfunc convention: non-zero when any
+     * entry of G is not finite */
+    for (long i = 0; i < P->N; ++i)
+        if (!isfinite(g[i])) return 1;
     return 0;
 }
 
@@ -833,8 +846,9 @@ int oracle_exprem_step(oracle_problem* P, double* t_io, double tend, const doubl
     /* g0 = G(u), reused from the previous accepted step when the caller
      * passes back the same state */
     if (!(P->cache_valid && P->cache_u == u && P->cache_t == t)) {
-        oracle_g(P, u, P->g0, nthreads);
+        int flag = oracle_g(P, u, P->g0, nthreads);
         st->FuncEvals++;
+        if (flag != 0) return 10;          /* G fails at the accepted state */
     }
     double* V = P->V;
     double* Hm = P->Hm;

@@ -107,6 +107,7 @@ _SIGNATURES = {
     "tsr_micro_mesh_free": (None, [C.POINTER(MicroMesh)]),
     "tsr_keff_free": (None, [C.POINTER(Keff)]),
     "tsr_phipade": (C.c_int, [dp, dp, C.c_double, C.c_int, C.c_int]),
+    "tsr_calibrate_micro_boundary": (C.c_int, [C.POINTER(UserData), C.POINTER(ModelExt), dp]),
     "tsr_init": (C.c_void_p, [C.POINTER(UserData), C.POINTER(ModelExt), C.c_void_p, C.c_int]),
     "tsr_free": (None, [C.c_void_p]),
     "tsr_stream": (C.c_void_p, [C.c_void_p]),
@@ -166,6 +167,8 @@ def ptr(a):
     """double* / int* of a contiguous numpy array (or NULL for None)."""
     if a is None:
         return None
+    if not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("array passed to the C-ABI must be C-contiguous")
     if a.dtype == np.float64:
         return a.ctypes.data_as(dp)
     if a.dtype == np.int32:

@@ -699,3 +699,43 @@ extern "C" int tsr_phipade(double* phiH, const double* H, double alpha, int m, i
     if (rc == TSR_ERR_SINGULAR) set_error("phipade: singular Pade denominator");
     return rc;
 }
+
+// ---- solution calibration --------------------------------------------------
+// The micro boundary unknowns are not evolved (G is 0 there; the cell sees
+// the macro interpolant instead), so, as src/save_solution.cpp:256-318 does
+// before writing, their stored values are overwritten with the macro
+// interpolant at centroid_k + s vectors_l (model_type 1: the centroid).
+
+extern "C" int tsr_calibrate_micro_boundary(const user_data_struct* ud, const tsr_model_ext* ext,
+                                            double* u)
+{
+    if (!ud || !u) return TSR_ERR_ARG;
+    const macro_mesh_struct& M = ud->macro_mesh;
+    const micro_mesh_struct& m = ud->micro_mesh;
+    const int nv = M.no_verts, Ne = M.no_elements, Mn = M.no_nodes, mn = m.no_nodes;
+    const double* scale = ext ? ext->cell_scale : nullptr;
+    for (int k = 0; k < Ne; ++k) {
+        double al[4];
+        for (int q = 0; q < nv; ++q) {
+            double a = M.shape_funcs[(size_t)(q * nv) * Ne + k] * u[M.elements[k]];
+            for (int i = 1; i < nv; ++i)
+                a = std::fma(M.shape_funcs[(size_t)(q * nv + i) * Ne + k],
+                             u[M.elements[(size_t)i * Ne + k]], a);
+            al[q] = a;
+        }
+        const double s = scale ? scale[k] : 1.0;
+        const double cx = M.centroid_elements[k], cy = M.centroid_elements[Ne + k];
+        for (int l = 0; l < mn; ++l) {
+            if (m.boundary_nodes[l] != 1) continue;
+            double px = cx, py = cy;
+            if (ud->model_type != 1) {
+                px = std::fma(s, m.vectors[l], cx);
+                py = std::fma(s, m.vectors[mn + l], cy);
+            }
+            double v = (nv == 3) ? std::fma(al[0], px, std::fma(al[1], py, al[2]))
+                                 : std::fma(al[0], px, std::fma(al[1], py, std::fma(al[2], px * py, al[3])));
+            u[(size_t)Mn + (size_t)k * mn + l] = v;
+        }
+    }
+    return TSR_OK;
+}

@@ -59,14 +59,17 @@ __device__ __forceinline__ void vg_full(double h, const VGPar& p, const tsr_math
         double a = p.alpha * ah;
         double L = tsr_log(a, T);
         double nL = p.n * L;
-        double t = tsr_exp(nL, T);
-        double s1 = 1.0 + t;
-        double l1 = tsr_log1p_s(t, s1, T);
+        double e = tsr_exp(-fabs(nL), T);           // min(t, 1/t)
+        double s1 = 1.0 + e;
+        double lp = tsr_log1p_s(e, s1, T);
+        const bool dry = nL >= 0.0;
+        double l1 = dry ? nL + lp : lp;             // log(1+t)
+        double y = dry ? -(p.m * lp) : p.m * (nL - lp);
         double X = tsr_exp(p.mh * l1, T);
         double Se = X * X;
-        double B = -tsr_expm1(p.m * (nL - l1), T);
+        double B = -tsr_expm1(y, T);
         K = (p.Ks * X) * (B * B);
-        Cn = p.coefC * (t * Se);
+        Cn = dry ? p.coefC * Se : p.coefC * (e * Se);
         Cd = ah * s1;
     } else {
         K = p.Ks;
@@ -83,12 +86,14 @@ __device__ __forceinline__ void vg_storage(double h, const VGPar& p, const tsr_m
         double a = p.alpha * ah;
         double L = tsr_log(a, T);
         double nL = p.n * L;
-        double t = tsr_exp(nL, T);
-        double s1 = 1.0 + t;
-        double l1 = tsr_log1p_s(t, s1, T);
+        double e = tsr_exp(-fabs(nL), T);
+        double s1 = 1.0 + e;
+        double lp = tsr_log1p_s(e, s1, T);
+        const bool dry = nL >= 0.0;
+        double l1 = dry ? nL + lp : lp;
         double X = tsr_exp(p.mh * l1, T);
         double Se = X * X;
-        Cn = p.coefC * (t * Se);
+        Cn = dry ? p.coefC * Se : p.coefC * (e * Se);
         Cd = ah * s1;
     } else {
         Cn = 0.0;
@@ -103,9 +108,10 @@ __device__ __forceinline__ double vg_se(double h, const VGPar& p, const tsr_math
     double a = p.alpha * ah;
     double L = tsr_log(a, T);
     double nL = p.n * L;
-    double t = tsr_exp(nL, T);
-    double s1 = 1.0 + t;
-    double l1 = tsr_log1p_s(t, s1, T);
+    double e = tsr_exp(-fabs(nL), T);
+    double s1 = 1.0 + e;
+    double lp = tsr_log1p_s(e, s1, T);
+    double l1 = nL >= 0.0 ? nL + lp : lp;
     double X = tsr_exp(p.mh * l1, T);
     return X * X;
 }
