@@ -273,7 +273,7 @@ def run_ours(args):
     gs_gbs = sbytes.value / max(sms.value * 1e-3, 1e-30) / 1e9
     # FP64 instructions per G from the instruction counts of the cell and
     # macro-node kernels (ncu, per unknown) -- see the kernel profiles
-    fp64_per_unknown = FP64_OPS_PER_UNKNOWN.get((args.n_macro, args.n_micro))
+    fp64_per_unknown = FP64_OPS_PER_UNKNOWN.get(args.n_micro)
     fp64 = None
     if fp64_per_unknown:
         ach = fp64_per_unknown * N / (g_avg_ms * 1e-3)
@@ -319,7 +319,7 @@ def run_ours(args):
                "sample": "%d G evaluations of the full workload by the oracle's OpenMP "
                          "Gfunc_parallel form with C-library log/exp (%.1f s)"
                          % (args.cpu_evals, el)}
-    traffic = G_TRAFFIC_PER_UNKNOWN.get((args.n_macro, args.n_micro))
+    traffic = G_TRAFFIC_PER_UNKNOWN.get(args.n_micro)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": WORLD, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_max / max(args.steps, 1),
@@ -353,11 +353,13 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-# FP64 instructions (DADD + DMUL + DFMA, thread level) per unknown of one G
-# evaluation, and DRAM bytes per unknown of one G launch, from the ncu
-# captures summarised in profiles/ (scaled by the unknowns processed).
-FP64_OPS_PER_UNKNOWN = {}
-G_TRAFFIC_PER_UNKNOWN = {}
+# FP64 instructions (DADD + DMUL + DFMA, thread level) per unknown of one
+# finite-difference Jv launch of the cell kernel, and its DRAM bytes (read +
+# write) per unknown, from the ncu capture of the 141x141 / 21x21 case in
+# profiles/k_cells_jv_141x141_21x21.md; both depend on the micro template
+# (21x21 nodes), not on the macro size, and are scaled by the unknowns.
+FP64_OPS_PER_UNKNOWN = {21: 97.13}
+G_TRAFFIC_PER_UNKNOWN = {21: 30.59}
 
 
 def main():

@@ -61,6 +61,7 @@ static const tsr_math_tables T = TSR_MATH_TABLES_INIT;
 #define tsr_exp(x, t) exp(x)
 #define tsr_expm1(x, t) expm1(x)
 #define tsr_log1p_s(x, s, t) log1p(x)
+#define tsr_log1p_unit(x, s1p, t) (*(s1p) = 1.0 + (x), log1p(x))
 #endif
 
 /* ------------------------------------------------------------------ */
@@ -107,8 +108,8 @@ static void vg_eval(double h, const vgpar* p, double* K, double* Cn, double* Cd,
         double L = tsr_log(a, &T);
         double nL = p->n * L;
         double e = tsr_exp(-fabs(nL), &T);
-        double s1 = 1.0 + e;
-        double lp = tsr_log1p_s(e, s1, &T);
+        double s1;
+        double lp = tsr_log1p_unit(e, &s1, &T);
         int dry = nL >= 0.0;
         double l1 = dry ? nL + lp : lp;                /* log(1+t) */
         double y = dry ? -(p->m * lp) : p->m * (nL - lp);
@@ -275,6 +276,7 @@ typedef struct oracle_problem {
     int kface;
     const double* cell_scale;
     unsigned char* dirichlet;   /* [Mn] */
+    double* faceD;              /* [9*mNe]: per SCV face j of element e, D1, D2, ny */
     long N;
     int Mn, Ne, nv, mn, mNe;
     /* EXPREM workspace */
@@ -310,6 +312,24 @@ oracle_problem* oracle_create(const user_data_struct* ud, const tsr_model_ext* e
     P->mNe = ud->micro_mesh.no_elements;
     P->N = (long)P->Mn + (long)P->Ne * P->mn;
     P->dirichlet = (unsigned char*)calloc((size_t)P->Mn, 1);
+    /* face coefficients: (grad h) . n = D1 (h1 - h0) + D2 (h2 - h0) with
+     * D_i = sfy_i ny + sfx_i nx (the gradient rows of the P1 interpolant
+     * dotted with the length-weighted face normal) */
+    {
+        const micro_mesh_struct* mm = &ud->micro_mesh;
+        const int mNe = mm->no_elements;
+        P->faceD = (double*)malloc(sizeof(double) * 9 * (size_t)mNe);
+        for (int e = 0; e < mNe; ++e)
+            for (int j = 0; j < 3; ++j) {
+                double nx = mm->normals[(size_t)(2 * j) * mNe + e];
+                double ny = mm->normals[(size_t)(2 * j + 1) * mNe + e];
+                for (int i = 1; i <= 2; ++i)
+                    P->faceD[(size_t)9 * e + 3 * j + i - 1] =
+                        fma(mm->shape_funcs[(size_t)(3 + i) * mNe + e], ny,
+                            mm->shape_funcs[(size_t)i * mNe + e] * nx);
+                P->faceD[(size_t)9 * e + 3 * j + 2] = ny;
+            }
+    }
     const macro_mesh_struct* M = &ud->macro_mesh;
     for (int k = 0; k < P->Ne; ++k)
         for (int j = 0; j < P->nv; ++j)
@@ -324,6 +344,7 @@ void oracle_destroy(oracle_problem* P)
 {
     if (!P) return;
     free(P->dirichlet);
+    free(P->faceD);
     free(P->V); free(P->Hm); free(P->phi); free(P->g0); free(P->g1); free(P->w);
     free(P->unew); free(P->winv); free(P->x); free(P->D); free(P->Dt);
     free(P);
@@ -416,20 +437,15 @@ static double micro_cell(const oracle_problem* P, const double* x, int k, double
     for (int e = 0; e < mNe; ++e) {
         int v[3];
         for (int j = 0; j < 3; ++j) v[j] = m->elements[(size_t)j * mNe + e];
-        double gx = m->shape_funcs[(size_t)0 * mNe + e] * h[v[0]];
-        gx = fma(m->shape_funcs[(size_t)1 * mNe + e], h[v[1]], gx);
-        gx = fma(m->shape_funcs[(size_t)2 * mNe + e], h[v[2]], gx);
-        double gy = m->shape_funcs[(size_t)3 * mNe + e] * h[v[0]];
-        gy = fma(m->shape_funcs[(size_t)4 * mNe + e], h[v[1]], gy);
-        gy = fma(m->shape_funcs[(size_t)5 * mNe + e], h[v[2]], gy);
-        /* cell scaled by s about the template: true gradient = g/s, true
-         * normal = s n, so (grad h + e_y).n = gx nx + (gy + s) ny */
-        double gys = gy + s;
+        /* (grad h + e_y).n through the face coefficients; a cell scaled by s
+         * about the template has gradient grad/s and normals s n, so the
+         * gravity term is s ny while D is scale-free */
+        double d1 = h[v[1]] - h[v[0]];
+        double d2 = h[v[2]] - h[v[0]];
+        const double* D = P->faceD + (size_t)9 * e;
         for (int j = 0; j < 3; ++j) {
             int a = v[j], b = v[(j + 1) % 3];
-            double nx = m->normals[(size_t)(2 * j) * mNe + e];
-            double ny = m->normals[(size_t)(2 * j + 1) * mNe + e];
-            double dot = fma(gx, nx, gys * ny);
+            double dot = fma(D[3 * j + 1], d2, fma(D[3 * j], d1, s * D[3 * j + 2]));
             double Kf;
             if (P->kface == 1)
                 Kf = (dot > 0.0) ? (2.0 * Kh[b]) : (2.0 * Kh[a]);
@@ -446,7 +462,11 @@ static double micro_cell(const oracle_problem* P, const double* x, int k, double
                     int vv = v[(j + sh) % 3];
                     double nbx = m->boundary_edge_normals[(size_t)(4 * j + 2 * sh) * mNe + e];
                     double nby = m->boundary_edge_normals[(size_t)(4 * j + 2 * sh + 1) * mNe + e];
-                    items[nitems++] = (2.0 * Kh[vv]) * fma(gx, nbx, gys * nby);
+                    double Db1 = fma(m->shape_funcs[(size_t)4 * mNe + e], nby,
+                                     m->shape_funcs[(size_t)1 * mNe + e] * nbx);
+                    double Db2 = fma(m->shape_funcs[(size_t)5 * mNe + e], nby,
+                                     m->shape_funcs[(size_t)2 * mNe + e] * nbx);
+                    items[nitems++] = (2.0 * Kh[vv]) * fma(Db2, d2, fma(Db1, d1, s * nby));
                 }
             }
         }

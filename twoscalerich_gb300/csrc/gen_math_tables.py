@@ -40,6 +40,8 @@ def main():
     out.append("#define TSR_LN2_N_LO %s" % float(ln2 / N - mpmath.mpf(float(ln2 / N))).hex())
     out.append("#define TSR_N_LN2 %s  /* %d / ln2 */" % (float(N / ln2).hex(), N))
     out.append("#define TSR_INV_LN10 %s  /* 1 / ln10 */" % float(1 / mpmath.log(10)).hex())
+    out.append("#define TSR_LN2_D %s  /* ln2 rounded to double */" % float(ln2).hex())
+    out.append("#define TSR_N_LN2_FIX54 %dULL  /* %d / ln2 * 2^54 */" % (rnd(N / ln2 * 2 ** 54), N))
     l42 = rnd(ln2 * 2 ** 42)
     out.append("#define TSR_LN2_HI42 %dLL  /* ln2 * 2^42, rounded */" % l42)
     out.append("#define TSR_LN2_R90 %dLL  /* (ln2 - TSR_LN2_HI42 * 2^-42) * 2^90 */"

@@ -268,16 +268,23 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
     T.mNe = mNe;
     {
         std::vector<int> ev(3 * (size_t)mNe);
-        std::vector<double> eg(12 * (size_t)mNe);
+        std::vector<double> eg(9 * (size_t)mNe);
         std::vector<int> node, code, ebf((size_t)mNe, 0), ebc((size_t)mNe, 0), bv;
         std::vector<double> bn;
         for (int e = 0; e < mNe; ++e) {
             int v[3];
             for (int j = 0; j < 3; ++j) v[j] = ev[3 * (size_t)e + j] = m.elements[(size_t)j * mNe + e];
-            for (int r = 0; r < 6; ++r) eg[12 * (size_t)e + r] = m.shape_funcs[(size_t)r * mNe + e];
-            for (int j = 0; j < 3; ++j)
-                for (int d = 0; d < 2; ++d)
-                    eg[12 * (size_t)e + 6 + 2 * j + d] = m.normals[(size_t)(2 * j + d) * mNe + e];
+            // face coefficients: (grad h).n_j = D1 (h1 - h0) + D2 (h2 - h0),
+            // D_i = sfy_i ny_j + sfx_i nx_j
+            for (int j = 0; j < 3; ++j) {
+                const double nx = m.normals[(size_t)(2 * j) * mNe + e];
+                const double ny = m.normals[(size_t)(2 * j + 1) * mNe + e];
+                for (int i = 1; i <= 2; ++i)
+                    eg[9 * (size_t)e + 3 * j + i - 1] =
+                        std::fma(m.shape_funcs[(size_t)(3 + i) * mNe + e], ny,
+                                 m.shape_funcs[(size_t)i * mNe + e] * nx);
+                eg[9 * (size_t)e + 3 * j + 2] = ny;
+            }
             for (int j = 0; j < 3; ++j) {
                 node.push_back(v[j]);
                 code.push_back((3 * e + j) << 1);
@@ -289,8 +296,12 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
                 if (m.boundary_edges[(size_t)j * mNe + e] != 1) continue;
                 for (int sh = 0; sh < 2; ++sh) {
                     bv.push_back(v[(j + sh) % 3]);
-                    bn.push_back(m.boundary_edge_normals[(size_t)(4 * j + 2 * sh) * mNe + e]);
-                    bn.push_back(m.boundary_edge_normals[(size_t)(4 * j + 2 * sh + 1) * mNe + e]);
+                    const double nbx = m.boundary_edge_normals[(size_t)(4 * j + 2 * sh) * mNe + e];
+                    const double nby = m.boundary_edge_normals[(size_t)(4 * j + 2 * sh + 1) * mNe + e];
+                    for (int i = 1; i <= 2; ++i)
+                        bn.push_back(std::fma(m.shape_funcs[(size_t)(3 + i) * mNe + e], nby,
+                                              m.shape_funcs[(size_t)i * mNe + e] * nbx));
+                    bn.push_back(nby);
                 }
             }
             ebc[e] = (int)bv.size() - ebf[e];

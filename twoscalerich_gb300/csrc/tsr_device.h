@@ -20,7 +20,7 @@ struct MicroTpl {
     int mn, mNe, nb;
     int pad;
     const int* ev;          // [3*mNe]  vertices of element e at 3e+j
-    const double* eg;       // [12*mNe] per element: sfx0..2, sfy0..2, nx0, ny0, nx1, ny1, nx2, ny2
+    const double* eg;       // [9*mNe] per face j of element e: D1, D2, ny (see tsr_ctx.cu)
     const int* csr_ptr;     // [mn+1]
     const int* csr_ent;     // (3e+j)<<1 | (1 if subtracted)
     const int* bnode;       // [mn]
@@ -29,7 +29,7 @@ struct MicroTpl {
     const int* eb_first;    // [mNe] first boundary item of element e
     const int* eb_count;    // [mNe]
     const int* b_v;         // [nb] node of item
-    const double* b_n;      // [2*nb] outward length-weighted normal of item
+    const double* b_n;      // [3*nb] per item: D1, D2 and ny of its outward normal
 };
 
 // Macro mesh in the reference layout plus derived arrays.

@@ -60,8 +60,8 @@ __device__ __forceinline__ void vg_full(double h, const VGPar& p, const tsr_math
         double L = tsr_log(a, T);
         double nL = p.n * L;
         double e = tsr_exp(-fabs(nL), T);           // min(t, 1/t)
-        double s1 = 1.0 + e;
-        double lp = tsr_log1p_s(e, s1, T);
+        double s1;
+        double lp = tsr_log1p_unit(e, &s1, T);
         const bool dry = nL >= 0.0;
         double l1 = dry ? nL + lp : lp;             // log(1+t)
         double y = dry ? -(p.m * lp) : p.m * (nL - lp);
@@ -87,8 +87,8 @@ __device__ __forceinline__ void vg_storage(double h, const VGPar& p, const tsr_m
         double L = tsr_log(a, T);
         double nL = p.n * L;
         double e = tsr_exp(-fabs(nL), T);
-        double s1 = 1.0 + e;
-        double lp = tsr_log1p_s(e, s1, T);
+        double s1;
+        double lp = tsr_log1p_unit(e, &s1, T);
         const bool dry = nL >= 0.0;
         double l1 = dry ? nL + lp : lp;
         double X = tsr_exp(p.mh * l1, T);
@@ -109,8 +109,8 @@ __device__ __forceinline__ double vg_se(double h, const VGPar& p, const tsr_math
     double L = tsr_log(a, T);
     double nL = p.n * L;
     double e = tsr_exp(-fabs(nL), T);
-    double s1 = 1.0 + e;
-    double lp = tsr_log1p_s(e, s1, T);
+    double s1;
+    double lp = tsr_log1p_unit(e, &s1, T);
     double l1 = nL >= 0.0 ? nL + lp : lp;
     double X = tsr_exp(p.mh * l1, T);
     return X * X;
@@ -294,20 +294,14 @@ __global__ void __launch_bounds__(256) k_cells(Problem P, const double* __restri
         // elements: SCV face fluxes and inclusion-boundary exchange items
         for (int e = tid; e < mNe; e += bs) {
             const int v0 = P.m.ev[3 * e], v1 = P.m.ev[3 * e + 1], v2 = P.m.ev[3 * e + 2];
-            const double* G = P.m.eg + 12 * (long long)e;
-            const double h0 = h[v0], h1 = h[v1], h2 = h[v2];
-            double gx = G[0] * h0;
-            gx = fma(G[1], h1, gx);
-            gx = fma(G[2], h2, gx);
-            double gy = G[3] * h0;
-            gy = fma(G[4], h1, gy);
-            gy = fma(G[5], h2, gy);
-            const double gys = gy + s;
+            const double* G = P.m.eg + 9 * (long long)e;   // per face: D1, D2, ny
+            const double h0 = h[v0];
+            const double d1 = h[v1] - h0, d2 = h[v2] - h0;
             const int vv[3] = {v0, v1, v2};
 #pragma unroll
             for (int j = 0; j < 3; ++j) {
                 const int a = vv[j], b = vv[(j + 1) % 3];
-                double dot = fma(gx, G[6 + 2 * j], gys * G[7 + 2 * j]);
+                double dot = fma(G[3 * j + 1], d2, fma(G[3 * j], d1, s * G[3 * j + 2]));
                 double Kf;
                 if (P.kface == 1)
                     Kf = (dot > 0.0) ? (2.0 * Kh[b]) : (2.0 * Kh[a]);
@@ -321,8 +315,8 @@ __global__ void __launch_bounds__(256) k_cells(Problem P, const double* __restri
                     const int f0 = P.m.eb_first[e];
                     for (int q = 0; q < c; ++q) {
                         const int it = f0 + q;
-                        items[it] = (2.0 * Kh[P.m.b_v[it]]) *
-                                    fma(gx, P.m.b_n[2 * it], gys * P.m.b_n[2 * it + 1]);
+                        const double* B = P.m.b_n + 3 * (long long)it;   // Db1, Db2, nby
+                        items[it] = (2.0 * Kh[P.m.b_v[it]]) * fma(B[1], d2, fma(B[0], d1, s * B[2]));
                     }
                 }
             }

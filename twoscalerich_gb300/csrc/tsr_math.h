@@ -30,9 +30,10 @@
  * split into an exact multiple of 2^-42 and a remainder carried in fixed
  * point, so the result is rounded once.
  *
- * FP64 instructions per call: tsr_log 1 (2 near x = 1), tsr_log1p_s 3
- * (0 for t < 2^-8), tsr_exp 4, tsr_expm1 1 for |x| < 2^-8, else 5 (8 for
- * |x| < ln2/2, where the result cancels against 1).  Accuracy against
+ * FP64 instructions per call: tsr_log 1 (2 near x = 1), tsr_log1p_unit
+ * 1 (0 for e < 2^-8, plus 1 returning 1 + e), tsr_log1p_s 3, tsr_exp 2,
+ * tsr_expm1 1 for |x| < 2^-8, else 3 (6 for |x| < ln2/2, where the result
+ * cancels against 1).  Accuracy against
  * glibc: within 1 ulp (tested).
  *
  * Deliberate domain limits (documented, tested):
@@ -249,6 +250,32 @@ TSR_HD double tsr_log(double x, const tsr_math_tables* T)
  * two-scale model reuses s).  For t >= 2^-8 the rounding error of s is
  * recovered exactly (Fast2Sum ordered by magnitude) and folded into the
  * reduced argument; below, log1p(t) = t Q(t) directly. */
+/* log1p(e) for 0 <= e <= 1, also returning s1 = 1 + e rounded to double.
+ * For e >= 2^-8 the sum 1 + e is formed exactly in fixed point (scale
+ * 2^60; e >= 2^-8 has no bits below 2^-60), so the reduction needs no
+ * correction term and s1 costs no FP64 instruction. */
+TSR_HD double tsr_log1p_unit(double e, double* s1, const tsr_math_tables* T)
+{
+    uint64_t b = tsr_d2u(e);
+    if (b < 0x3F70000000000000ull) {                  /* e < 2^-8 */
+        *s1 = 1.0 + e;
+        if (e == 0.0) return e;
+        return tsr_log1p_small(e);
+    }
+    int ee = (int)(b >> 52);                           /* 1015 .. 1023 */
+    uint64_t S = (1ull << 60) + (((b & TSR_MANT_MASK) | (1ull << 52)) << (ee - 1015));
+    *s1 = tsr_fix2d((int64_t)S, 60);
+    if (S == (1ull << 61)) return TSR_LN2_D;           /* e = 1 */
+    /* S in (1, 2): c_i from the 8 bits below the leading one */
+    unsigned i = (unsigned)(S >> 52) & 0xFFu;
+    const tsr_log_entry* t = &T->lg[i];
+    uint64_t F = S & ((1ull << 52) - 1);               /* (S - c_i) * 2^60 */
+    int64_t U71 = (int64_t)tsr_umulhi(F << 12, t->invc63);
+    int64_t Q = tsr_log1p_q(tsr_sar(U71, 7));
+    int64_t lo = tsr_smulhi(U71, Q) + t->logc_r69;
+    return tsr_fix2d(t->logc_hi42, 42) + tsr_fix2d(lo, 69);
+}
+
 TSR_HD double tsr_log1p_s(double t, double s, const tsr_math_tables* T)
 {
     if (tsr_d2u(t) < 0x3F70000000000000ull) {          /* 0 <= t < 2^-8 */
@@ -266,13 +293,22 @@ TSR_HD double tsr_log1p(double t, const tsr_math_tables* T)
 }
 
 /* Shared reduction of exp/expm1: x = (k/256) ln2 + r, |r| <= ln2/512
- * (4 FP64 instructions); returns Q(r) = expm1(r)/r at scale 2^62 and sets
+ * (2 FP64 instructions); returns Q(r) = expm1(r)/r at scale 2^62 and sets
  * r, j = k mod 256 and M = (k - j)/256. */
 TSR_HD int64_t tsr_exp_reduce(double x, double* r_out, unsigned* j, int64_t* M, int64_t* k_out)
 {
-    double t = fma(x, TSR_N_LN2, TSR_SHIFTER);
-    int64_t k = (int64_t)(tsr_d2u(t) - TSR_SHIFTER_BITS);
-    double kd = t - TSR_SHIFTER;
+    /* k = round(x 256/ln2) on the integer pipe: (53-bit mantissa << 11)
+     * times 256/ln2 * 2^54, high word, shifted by the exponent (|x| < 707) */
+    uint64_t b = tsr_d2u(x);
+    int ex = (int)((b >> 52) & 0x7FF);
+    int sh = 1076 - ex;
+    int64_t k = 0;
+    if (sh < 64) {
+        uint64_t P = tsr_umulhi(((b & TSR_MANT_MASK) | (1ull << 52)) << 11, TSR_N_LN2_FIX54);
+        uint64_t a = (P + (1ull << (sh - 1))) >> sh;
+        k = (b >> 63) ? -(int64_t)a : (int64_t)a;
+    }
+    double kd = tsr_fix2d(k, 0);                                /* exact, |k| < 2^18 */
     double r = fma(-kd, TSR_LN2_N_HI, x);
     r = fma(-kd, TSR_LN2_N_LO, r);
     *j = (unsigned)k & 0xFFu;
