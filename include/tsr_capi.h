@@ -167,6 +167,14 @@ int tsr_set_default_ext(const tsr_model_ext* ext, int max_krylov);
 /* Releases every implicitly created context. */
 void tsr_release_all(void);
 
+/* Autotuner of the cell kernel (no counterpart in the reference): times G
+ * at state u_host (host, N doubles) for every block size and shared-memory
+ * budget that fits, packs cells into CTAs accordingly and keeps the fastest
+ * plan.  Plans only change how cells are grouped per CTA, never the
+ * results.  Outputs may be NULL. */
+int tsr_autotune(tsr_ctx* ctx, const double* u_host, int reps, double* best_ms,
+                 int* best_threads, int* best_budget);
+
 /* ---- measurement hooks (no reference counterpart) ---------------------- */
 
 /* Enable (1) or disable (0) CUDA-event timing of the kernel classes inside

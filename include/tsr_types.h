@@ -138,8 +138,16 @@ typedef struct tsr_model_ext {
     double dirichlet_h;          /* head on nodes of type-5 edges [m] */
     double specific_storage;     /* S_s added to C(h) [1/m]; <= 0 means 1e-6 */
     int    kface_mode;           /* micro face conductivity: 0 mean of the two nodes, 1 upwind */
-    int    reserved;
+    int    n_templates;          /* > 0: cells use per-cell micro templates (below) */
     const double* cell_scale;    /* [no_elements] inclusion scale per cell, NULL = all 1 */
+    /* Batched form (uneven micro meshes; no counterpart in the reference,
+     * whose user_data holds one micro mesh, include/user_data.h:4): with
+     * n_templates > 0, cell k uses templates[cell_template[k]] instead of
+     * user_data.micro_mesh, and the unknowns of cell k follow those of cell
+     * k-1 (offsets are prefix sums of the template node counts). */
+    const micro_mesh_struct* templates;   /* [n_templates] */
+    const int* cell_template;             /* [no_elements] */
+    const soil_struct* cell_soilB;        /* [no_elements] material B per cell, NULL = soilB */
 } tsr_model_ext;
 
 #endif /* TSR_TYPES_H */

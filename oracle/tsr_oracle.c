@@ -276,7 +276,15 @@ typedef struct oracle_problem {
     int kface;
     const double* cell_scale;
     unsigned char* dirichlet;   /* [Mn] */
-    double* faceD;              /* [9*mNe]: per SCV face j of element e, D1, D2, ny */
+    /* micro templates: one (user_data.micro_mesh) or, in the batched form,
+     * tsr_model_ext.templates with a template per cell */
+    int ntpl;
+    const micro_mesh_struct* tpl;       /* [ntpl] */
+    double** faceD;             /* [ntpl][9*mNe]: per SCV face j of element e, D1, D2, ny */
+    const int* cell_tpl;        /* [Ne] or NULL (all template 0) */
+    long* cell_off;             /* [Ne] first unknown of cell k */
+    vgpar* cell_pB;             /* [Ne] or NULL (all pB) */
+    int max_mn, max_mNe;
     long N;
     int Mn, Ne, nv, mn, mNe;
     /* EXPREM workspace */
@@ -290,7 +298,8 @@ typedef struct oracle_problem {
 
 oracle_problem* oracle_create(const user_data_struct* ud, const tsr_model_ext* ext)
 {
-    if (!ud || ud->micro_mesh.no_verts != 3) return NULL;
+    if (!ud) return NULL;
+    if (!(ext && ext->n_templates > 0) && ud->micro_mesh.no_verts != 3) return NULL;
     oracle_problem* P = (oracle_problem*)calloc(1, sizeof(oracle_problem));
     P->ud = *ud;
     P->pA = make_vgpar(&ud->soilA);
@@ -300,7 +309,6 @@ oracle_problem* oracle_create(const user_data_struct* ud, const tsr_model_ext* e
     P->kp.inv_logr = 1.0 / ud->effective_conductivity.logr;
     P->kp.Kv = ud->effective_conductivity.Keff_values;
     P->epsA = ud->effective_conductivity.epsilonA;
-    P->inv_Y = 1.0 / ud->micro_mesh.cell_area;
     P->Ss = (ext && ext->specific_storage > 0.0) ? ext->specific_storage : 1e-6;
     P->hD = ext ? ext->dirichlet_h : 0.0;
     P->kface = ext ? ext->kface_mode : 0;
@@ -310,24 +318,51 @@ oracle_problem* oracle_create(const user_data_struct* ud, const tsr_model_ext* e
     P->nv = ud->macro_mesh.no_verts;
     P->mn = ud->micro_mesh.no_nodes;
     P->mNe = ud->micro_mesh.no_elements;
-    P->N = (long)P->Mn + (long)P->Ne * P->mn;
     P->dirichlet = (unsigned char*)calloc((size_t)P->Mn, 1);
+    if (ext && ext->n_templates > 0) {
+        P->ntpl = ext->n_templates;
+        P->tpl = ext->templates;
+        P->cell_tpl = ext->cell_template;
+    } else {
+        P->ntpl = 1;
+        P->tpl = &P->ud.micro_mesh;
+        P->cell_tpl = NULL;
+    }
+    /* unknown offsets: cell k follows cell k-1 */
+    P->cell_off = (long*)malloc(sizeof(long) * (size_t)(P->Ne > 0 ? P->Ne : 1));
+    long off = P->Mn;
+    for (int k = 0; k < P->Ne; ++k) {
+        P->cell_off[k] = off;
+        off += P->tpl[P->cell_tpl ? P->cell_tpl[k] : 0].no_nodes;
+    }
+    P->N = off;
+    P->inv_Y = 1.0 / P->tpl[0].cell_area;
+    P->cell_pB = NULL;
+    if (ext && ext->cell_soilB) {
+        P->cell_pB = (vgpar*)malloc(sizeof(vgpar) * (size_t)P->Ne);
+        for (int k = 0; k < P->Ne; ++k) P->cell_pB[k] = make_vgpar(&ext->cell_soilB[k]);
+    }
     /* face coefficients: (grad h) . n = D1 (h1 - h0) + D2 (h2 - h0) with
      * D_i = sfy_i ny + sfx_i nx (the gradient rows of the P1 interpolant
      * dotted with the length-weighted face normal) */
-    {
-        const micro_mesh_struct* mm = &ud->micro_mesh;
+    P->faceD = (double**)malloc(sizeof(double*) * (size_t)P->ntpl);
+    P->max_mn = 0;
+    P->max_mNe = 0;
+    for (int t = 0; t < P->ntpl; ++t) {
+        const micro_mesh_struct* mm = &P->tpl[t];
         const int mNe = mm->no_elements;
-        P->faceD = (double*)malloc(sizeof(double) * 9 * (size_t)mNe);
+        if (mm->no_nodes > P->max_mn) P->max_mn = mm->no_nodes;
+        if (mNe > P->max_mNe) P->max_mNe = mNe;
+        P->faceD[t] = (double*)malloc(sizeof(double) * 9 * (size_t)mNe);
         for (int e = 0; e < mNe; ++e)
             for (int j = 0; j < 3; ++j) {
                 double nx = mm->normals[(size_t)(2 * j) * mNe + e];
                 double ny = mm->normals[(size_t)(2 * j + 1) * mNe + e];
                 for (int i = 1; i <= 2; ++i)
-                    P->faceD[(size_t)9 * e + 3 * j + i - 1] =
+                    P->faceD[t][(size_t)9 * e + 3 * j + i - 1] =
                         fma(mm->shape_funcs[(size_t)(3 + i) * mNe + e], ny,
                             mm->shape_funcs[(size_t)i * mNe + e] * nx);
-                P->faceD[(size_t)9 * e + 3 * j + 2] = ny;
+                P->faceD[t][(size_t)9 * e + 3 * j + 2] = ny;
             }
     }
     const macro_mesh_struct* M = &ud->macro_mesh;
@@ -344,7 +379,10 @@ void oracle_destroy(oracle_problem* P)
 {
     if (!P) return;
     free(P->dirichlet);
+    for (int t = 0; t < P->ntpl; ++t) free(P->faceD[t]);
     free(P->faceD);
+    free(P->cell_off);
+    free(P->cell_pB);
     free(P->V); free(P->Hm); free(P->phi); free(P->g0); free(P->g1); free(P->w);
     free(P->unew); free(P->winv); free(P->x); free(P->D); free(P->Dt);
     free(P);
@@ -395,10 +433,12 @@ static void interp_grad(int nv, const double al[4], double x, double y, double* 
  * into the inclusion.  x is the macro+micro state. */
 static double micro_cell(const oracle_problem* P, const double* x, int k, double* g, double* scratch)
 {
-    const micro_mesh_struct* m = &P->ud.micro_mesh;
+    const int t = P->cell_tpl ? P->cell_tpl[k] : 0;
+    const micro_mesh_struct* m = &P->tpl[t];
     const macro_mesh_struct* M = &P->ud.macro_mesh;
-    const int mn = P->mn, mNe = P->mNe, Ne = P->Ne;
-    const long off = (long)P->Mn + (long)k * mn;
+    const int mn = m->no_nodes, mNe = m->no_elements, Ne = P->Ne;
+    const long off = P->cell_off[k];
+    const vgpar* pB = P->cell_pB ? &P->cell_pB[k] : &P->pB;
     const double s = P->cell_scale ? P->cell_scale[k] : 1.0;
     const double s2 = s * s;
     double* h = scratch;
@@ -429,7 +469,7 @@ static double micro_cell(const oracle_problem* P, const double* x, int k, double
         }
         h[l] = hl;
         double K, Se;
-        vg_eval(hl, &P->pB, &K, &Cn[l], &Cd[l], &Se);
+        vg_eval(hl, pB, &K, &Cn[l], &Cd[l], &Se);
         Kh[l] = 0.5 * K;
         acc[l] = 0.0;
     }
@@ -442,7 +482,7 @@ static double micro_cell(const oracle_problem* P, const double* x, int k, double
          * gravity term is s ny while D is scale-free */
         double d1 = h[v[1]] - h[v[0]];
         double d2 = h[v[2]] - h[v[0]];
-        const double* D = P->faceD + (size_t)9 * e;
+        const double* D = P->faceD[t] + (size_t)9 * e;
         for (int j = 0; j < 3; ++j) {
             int a = v[j], b = v[(j + 1) % 3];
             double dot = fma(D[3 * j + 1], d2, fma(D[3 * j], d1, s * D[3 * j + 2]));
@@ -492,7 +532,7 @@ static double micro_cell(const oracle_problem* P, const double* x, int k, double
 
 static size_t scratch_doubles(const oracle_problem* P)
 {
-    return (size_t)5 * P->mn + (size_t)6 * P->mNe + 64;
+    return (size_t)5 * P->max_mn + (size_t)6 * P->max_mNe + 64;
 }
 
 /* g = G(x).  nthreads > 1: the micro cells run as an OpenMP loop (the
@@ -618,8 +658,7 @@ int oracle_jv(oracle_problem* P, const double* u, const double* g0, const double
 int oracle_water(oracle_problem* P, const double* u, double* water)
 {
     const macro_mesh_struct* M = &P->ud.macro_mesh;
-    const micro_mesh_struct* m = &P->ud.micro_mesh;
-    const int Mn = P->Mn, Ne = P->Ne, mn = P->mn, nv = P->nv;
+    const int Mn = P->Mn, Ne = P->Ne, nv = P->nv;
     double* terms = (double*)malloc(sizeof(double) * (size_t)(Mn + Ne));
     for (int i = 0; i < Mn; ++i) {
         double K, Cn, Cd, Se;
@@ -628,6 +667,9 @@ int oracle_water(oracle_problem* P, const double* u, double* water)
     }
     for (int k = 0; k < Ne; ++k) {
         const double s = P->cell_scale ? P->cell_scale[k] : 1.0;
+        const micro_mesh_struct* m = &P->tpl[P->cell_tpl ? P->cell_tpl[k] : 0];
+        const int mn = m->no_nodes;
+        const vgpar* pB = P->cell_pB ? &P->cell_pB[k] : &P->pB;
         double al[4];
         interp_coeffs(P, u, k, al);
         double cx = M->centroid_elements[k], cy = M->centroid_elements[Ne + k];
@@ -643,11 +685,11 @@ int oracle_water(oracle_problem* P, const double* u, double* water)
                 }
                 hl = interp_at(nv, al, px, py);
             } else {
-                hl = u[(long)Mn + (long)k * mn + l];
+                hl = u[P->cell_off[k] + l];
             }
             double K, Cn, Cd, Se;
-            vg_eval(hl, &P->pB, &K, &Cn, &Cd, &Se);
-            p[l & 31] += fma(P->pB.dth, Se, P->pB.thr) * m->CV_area[l];
+            vg_eval(hl, pB, &K, &Cn, &Cd, &Se);
+            p[l & 31] += fma(pB->dth, Se, pB->thr) * m->CV_area[l];
         }
         double area = M->SCV_area[k];
         for (int j = 1; j < nv; ++j) area += M->SCV_area[(size_t)j * Ne + k];

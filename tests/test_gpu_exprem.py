@@ -55,6 +55,13 @@ def test_trajectory_config2_small_scaled_cells():
     _compare(p)
 
 
+def test_trajectory_config3_batched_uneven_cells():
+    p = P.config3(n_macro=11)
+    p.tend = 0.05
+    p.tspan = np.concatenate([[2.0], [0.025, 0.05]])
+    _compare(p)
+
+
 def test_device_resident_stepping_matches_host_stepping():
     p = P.config1()
     p.tend = 0.05

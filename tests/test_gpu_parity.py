@@ -26,6 +26,7 @@ def cases():
         "config1_upwind": lambda: P.config1(kface=1),
         "fixture10_quads": lambda: P.fixture10(),
         "config2_small": lambda: P.config2(n_macro=21, n_micro=9),
+        "config3_batched": lambda: P.config3(n_macro=21),
     }
 
 
@@ -84,3 +85,14 @@ def test_water_content():
     ctx = P.Context(p, max_krylov=0)
     orc = oracle.Oracle(p)
     assert ctx.water(p.u0) == orc.water(p.u0)
+
+
+def test_autotuned_packings_give_identical_bits():
+    """Every packing of cells into CTAs the autotuner tries gives the same G."""
+    p = P.config3(n_macro=31)
+    ctx = P.Context(p, max_krylov=0)
+    g_default = ctx.g(p.u0)
+    ms, thr, bud = ctx.autotune(p.u0, reps=2)
+    assert ms > 0 and thr in (128, 256) and bud >= 48 * 1024
+    assert np.array_equal(ctx.g(p.u0), g_default)
+    assert np.array_equal(g_default, oracle.Oracle(p, nthreads=8).g(p.u0))

@@ -19,20 +19,24 @@ from twoscalerich_gb300 import problem as P
 
 def hydrostatic_state(p, c):
     """h = c - y at every macro node and every micro node (physical y)."""
-    Mn, Ne, mn = p.Mn, p.Ne, p.mn
+    Mn, Ne = p.Mn, p.Ne
     xy = p.array("nodes", 2 * Mn)
     u = np.empty(p.N)
     u[:Mn] = c - xy[Mn:]
     cent = p.array("centroid_elements", 2 * Ne)
-    vec = capi.as_array(p.micro.vectors, 2 * mn)
     s = p._scale if p._scale is not None else np.ones(Ne)
-    ys = cent[Ne:][:, None] + s[:, None] * vec[mn:][None, :]
-    u[Mn:] = (c - ys).ravel()
+    for k in range(Ne):
+        m = p._tpl[p.cell_template[k]] if p.cell_template is not None else p.micro
+        mn = m.no_nodes
+        vec = capi.as_array(m.vectors, 2 * mn)
+        off = int(p.cell_off[k])
+        u[off:off + mn] = c - (cent[Ne + k] + s[k] * vec[mn:])
     return u
 
 
 @pytest.mark.parametrize("make", [lambda: P.config2(n_macro=11, n_micro=7),
-                                  lambda: P.fixture10(boundary_flux=0.0)])
+                                  lambda: P.fixture10(boundary_flux=0.0),
+                                  lambda: P.config3(n_macro=9)])
 def test_hydrostatic_equilibrium_is_stationary(make):
     p = make()
     c = -3.0

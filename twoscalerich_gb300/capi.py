@@ -82,7 +82,9 @@ class ExpremStats(C.Structure):
 class ModelExt(C.Structure):
     _fields_ = [
         ("dirichlet_h", C.c_double), ("specific_storage", C.c_double),
-        ("kface_mode", C.c_int), ("reserved", C.c_int), ("cell_scale", dp),
+        ("kface_mode", C.c_int), ("n_templates", C.c_int), ("cell_scale", dp),
+        ("templates", C.POINTER(MicroMesh)), ("cell_template", ip),
+        ("cell_soilB", C.POINTER(Soil)),
     ]
 
 
@@ -128,6 +130,7 @@ _SIGNATURES = {
     "tsr_gfunc_gpu": (C.c_int, [dp, dp, C.POINTER(UserData)]),
     "tsr_set_default_ext": (C.c_int, [C.POINTER(ModelExt), C.c_int]),
     "tsr_release_all": (None, []),
+    "tsr_autotune": (C.c_int, [C.c_void_p, dp, C.c_int, dp, ip, ip]),
     "tsr_profile": (C.c_int, [C.c_void_p, C.c_int]),
     "tsr_profile_read": (C.c_int, [C.c_void_p, C.c_int, dp, C.POINTER(C.c_longlong), dp]),
     "tsr_kernel_launches": (C.c_ulonglong, []),

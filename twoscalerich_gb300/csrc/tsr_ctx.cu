@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -70,6 +71,12 @@ struct tsr_ctx {
     std::vector<ProfEv> prof_ev;
     size_t prof_used = 0;
     cudaEvent_t marks[16] = {};
+    // cell kernel planning (templates, bundles, launch shape)
+    std::vector<TplDesc> tpl_host;
+    std::vector<int> cell_tpl_host;
+    int* d_bundle = nullptr;     // 3 * Ne ints (tpl, first, count) + Ne cell ids
+    int nsm = 0, dev_smem = 0;
+    int tuned_threads = 0, tuned_budget = 0;
 };
 
 namespace {
@@ -139,16 +146,100 @@ Csr group_events(int n_nodes, const std::vector<int>& node, const std::vector<in
     return c;
 }
 
+
+constexpr int kMiscSlots = 32;     // most cells in one bundle
+
+// shared memory of a bundle plan: tables, per-cell scratch, the largest
+// bundle's state
+size_t cell_smem(int slots, size_t state_doubles)
+{
+    return sizeof(tsr_math_tables) + sizeof(double) * 16 * (size_t)slots +
+           (sizeof(long long) + 2 * sizeof(int)) * (size_t)slots + sizeof(double) * state_doubles;
+}
+
+}  // namespace
+
+namespace tsr {
+
+// Packs cells into bundles (cells of one template, as many as fit in the
+// shared-memory budget, at most kMiscSlots), largest templates first, and
+// sets the persistent grid of the cell kernel for `threads` per CTA.
+int plan_cells(tsr_ctx* c, int threads, int budget)
+{
+    Problem& P = c->P;
+    const int ntpl = (int)c->tpl_host.size();
+    const size_t fixed = cell_smem(kMiscSlots, 0);
+    std::vector<int> per(ntpl, 1);
+    size_t max_state = 0;
+    for (int t = 0; t < ntpl; ++t) {
+        const size_t st = (size_t)c->tpl_host[t].state;
+        long long fit = budget > (long long)fixed ? ((long long)budget - (long long)fixed) / (long long)(8 * st) : 0;
+        if (fit < 1) fit = 1;
+        if (fit > kMiscSlots) fit = kMiscSlots;
+        per[t] = (int)fit;
+        if ((size_t)per[t] * st > max_state) max_state = (size_t)per[t] * st;
+    }
+    const size_t smem = cell_smem(kMiscSlots, max_state);
+    if (smem > (size_t)c->dev_smem) {
+        set_error("a micro cell does not fit in shared memory");
+        return TSR_ERR_ARG;
+    }
+    // cells grouped by template, bundles of per[t] cells
+    std::vector<std::vector<int>> cells(ntpl);
+    for (int k = 0; k < c->Ne; ++k) cells[c->cell_tpl_host[k]].push_back(k);
+    std::vector<int> order(ntpl);
+    for (int t = 0; t < ntpl; ++t) order[t] = t;
+    std::sort(order.begin(), order.end(),
+              [&](int a, int b) { return c->tpl_host[a].state > c->tpl_host[b].state; });
+    std::vector<int> btpl, bfirst, bcount, bcells;
+    for (int t : order) {
+        const std::vector<int>& cl = cells[t];
+        for (size_t i = 0; i < cl.size(); i += (size_t)per[t]) {
+            const int n = (int)std::min((size_t)per[t], cl.size() - i);
+            btpl.push_back(t);
+            bfirst.push_back((int)bcells.size());
+            bcount.push_back(n);
+            for (int q = 0; q < n; ++q) bcells.push_back(cl[i + q]);
+        }
+    }
+    const int nbun = (int)btpl.size();
+    std::vector<int> buf;
+    buf.reserve(3 * (size_t)nbun + bcells.size());
+    buf.insert(buf.end(), btpl.begin(), btpl.end());
+    buf.insert(buf.end(), bfirst.begin(), bfirst.end());
+    buf.insert(buf.end(), bcount.begin(), bcount.end());
+    buf.insert(buf.end(), bcells.begin(), bcells.end());
+    CK(cudaMemcpy(c->d_bundle, buf.data(), sizeof(int) * buf.size(), cudaMemcpyHostToDevice));
+    MicroSet& S = P.m;
+    S.n_bundles = nbun;
+    S.bundle_tpl = c->d_bundle;
+    S.bundle_first = c->d_bundle + nbun;
+    S.bundle_count = c->d_bundle + 2 * nbun;
+    S.bundle_cells = c->d_bundle + 3 * nbun;
+    S.maxc = *std::max_element(per.begin(), per.end());
+    P.misc_slots = kMiscSlots;
+    P.micro_block = threads;
+    P.micro_smem = smem;
+    int occ = 1;
+    int rc = configure_cell_kernels(P, &occ);
+    if (rc) return rc;
+    long long grid = (long long)occ * c->nsm;
+    P.micro_grid = (int)(grid < nbun ? grid : nbun);
+    if (P.micro_grid < 1) P.micro_grid = 1;
+    c->tuned_threads = threads;
+    c->tuned_budget = budget;
+    return TSR_OK;
+}
+
+}  // namespace tsr
+
+namespace {
+
 int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* ext)
 {
     const macro_mesh_struct& M = ud.macro_mesh;
-    const micro_mesh_struct& m = ud.micro_mesh;
     if (M.no_verts != 3 && M.no_verts != 4) {
         set_error("macro mesh must have 3 or 4 vertices per element");
-        return TSR_ERR_ARG;
-    }
-    if (m.no_verts != 3) {
-        set_error("micro mesh must be triangular");
         return TSR_ERR_ARG;
     }
     if (ud.model_type < 1 || ud.model_type > 3) {
@@ -156,8 +247,39 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
         return TSR_ERR_ARG;
     }
     const int nv = M.no_verts, Ne = M.no_elements, Mn = M.no_nodes;
-    const int mn = m.no_nodes, mNe = m.no_elements;
-    const long long N = (long long)Mn + (long long)Ne * mn;
+    // micro templates: the one micro mesh, or one per cell (batched form)
+    const bool batched = ext && ext->n_templates > 0;
+    const int ntpl = batched ? ext->n_templates : 1;
+    const micro_mesh_struct* tpls = batched ? ext->templates : &ud.micro_mesh;
+    if (batched && (!ext->templates || !ext->cell_template)) {
+        set_error("batched form needs templates and cell_template");
+        return TSR_ERR_ARG;
+    }
+    for (int t = 0; t < ntpl; ++t) {
+        const micro_mesh_struct& m = tpls[t];
+        if (m.no_verts != 3) {
+            set_error("micro meshes must be triangular");
+            return TSR_ERR_ARG;
+        }
+        for (long long i = 0; i < 3LL * m.no_elements; ++i)
+            if (m.elements[i] < 0 || m.elements[i] >= m.no_nodes) {
+                set_error("micro element index out of range");
+                return TSR_ERR_BOUNDS;
+            }
+    }
+    c->cell_tpl_host.assign((size_t)Ne, 0);
+    std::vector<long long> cell_off((size_t)Ne);
+    long long N = Mn;
+    for (int k = 0; k < Ne; ++k) {
+        int t = batched ? ext->cell_template[k] : 0;
+        if (t < 0 || t >= ntpl) {
+            set_error("cell_template out of range");
+            return TSR_ERR_BOUNDS;
+        }
+        c->cell_tpl_host[k] = t;
+        cell_off[k] = N;
+        N += tpls[t].no_nodes;
+    }
     if (N > 0x7fffffffLL || (long long)Ne * 32 > 0x7fffffffLL) {
         set_error("problem too large for 32-bit indices");
         return TSR_ERR_ARG;
@@ -169,11 +291,6 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
     for (long long i = 0; i < (long long)nv * Ne; ++i)
         if (M.elements[i] < 0 || M.elements[i] >= Mn) {
             set_error("macro element index out of range");
-            return TSR_ERR_BOUNDS;
-        }
-    for (long long i = 0; i < 3LL * mNe; ++i)
-        if (m.elements[i] < 0 || m.elements[i] >= mn) {
-            set_error("micro element index out of range");
             return TSR_ERR_BOUNDS;
         }
     c->N = N;
@@ -252,7 +369,7 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
     D.keff_first = K.logh_first;
     D.keff_inv_logr = 1.0 / K.logr;
     D.epsA = K.epsilonA;
-    D.inv_Y = 1.0 / m.cell_area;
+    D.inv_Y = 1.0 / tpls[0].cell_area;
     D.Ss = (ext && ext->specific_storage > 0.0) ? ext->specific_storage : 1e-6;
     D.bflux = ud.boundary_flux;
     P.pA = make_vg(ud.soilA);
@@ -262,63 +379,101 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
     if (ext && ext->cell_scale) {
         if ((rc = upload(c, ext->cell_scale, (size_t)Ne, &P.cell_scale))) return rc;
     }
-    // micro template
-    MicroTpl& T = P.m;
-    T.mn = mn;
-    T.mNe = mNe;
+    // micro templates, concatenated
+    MicroSet& S = P.m;
+    S.ntpl = ntpl;
     {
-        std::vector<int> ev(3 * (size_t)mNe);
-        std::vector<double> eg(9 * (size_t)mNe);
-        std::vector<int> node, code, ebf((size_t)mNe, 0), ebc((size_t)mNe, 0), bv;
-        std::vector<double> bn;
-        for (int e = 0; e < mNe; ++e) {
-            int v[3];
-            for (int j = 0; j < 3; ++j) v[j] = ev[3 * (size_t)e + j] = m.elements[(size_t)j * mNe + e];
-            // face coefficients: (grad h).n_j = D1 (h1 - h0) + D2 (h2 - h0),
-            // D_i = sfy_i ny_j + sfx_i nx_j
-            for (int j = 0; j < 3; ++j) {
-                const double nx = m.normals[(size_t)(2 * j) * mNe + e];
-                const double ny = m.normals[(size_t)(2 * j + 1) * mNe + e];
-                for (int i = 1; i <= 2; ++i)
-                    eg[9 * (size_t)e + 3 * j + i - 1] =
-                        std::fma(m.shape_funcs[(size_t)(3 + i) * mNe + e], ny,
-                                 m.shape_funcs[(size_t)i * mNe + e] * nx);
-                eg[9 * (size_t)e + 3 * j + 2] = ny;
-            }
-            for (int j = 0; j < 3; ++j) {
-                node.push_back(v[j]);
-                code.push_back((3 * e + j) << 1);
-                node.push_back(v[(j + 1) % 3]);
-                code.push_back(((3 * e + j) << 1) | 1);
-            }
-            ebf[e] = (int)bv.size();
-            for (int j = 0; j < 3; ++j) {
-                if (m.boundary_edges[(size_t)j * mNe + e] != 1) continue;
-                for (int sh = 0; sh < 2; ++sh) {
-                    bv.push_back(v[(j + sh) % 3]);
-                    const double nbx = m.boundary_edge_normals[(size_t)(4 * j + 2 * sh) * mNe + e];
-                    const double nby = m.boundary_edge_normals[(size_t)(4 * j + 2 * sh + 1) * mNe + e];
-                    for (int i = 1; i <= 2; ++i)
-                        bn.push_back(std::fma(m.shape_funcs[(size_t)(3 + i) * mNe + e], nby,
-                                              m.shape_funcs[(size_t)i * mNe + e] * nbx));
-                    bn.push_back(nby);
+        std::vector<int> ev, cptr, cent, bnode, ebf, ebc, bv;
+        std::vector<double> eg, cv, vec, bn;
+        c->tpl_host.clear();
+        for (int t = 0; t < ntpl; ++t) {
+            const micro_mesh_struct& m = tpls[t];
+            const int mn = m.no_nodes, mNe = m.no_elements;
+            TplDesc d{};
+            d.mn = mn;
+            d.mNe = mNe;
+            d.ev = (int)ev.size();
+            d.eg = (int)eg.size();
+            d.csr_ptr = (int)cptr.size();
+            d.csr_ent = (int)cent.size();
+            d.node = (int)bnode.size();
+            d.bitem = (int)bv.size();
+            std::vector<int> node, code;
+            for (int e = 0; e < mNe; ++e) {
+                int v[3];
+                for (int j = 0; j < 3; ++j) {
+                    v[j] = m.elements[(size_t)j * mNe + e];
+                    ev.push_back(v[j]);
                 }
+                // face coefficients: (grad h).n_j = D1 (h1 - h0) + D2 (h2 - h0),
+                // D_i = sfy_i ny_j + sfx_i nx_j
+                for (int j = 0; j < 3; ++j) {
+                    const double nx = m.normals[(size_t)(2 * j) * mNe + e];
+                    const double ny = m.normals[(size_t)(2 * j + 1) * mNe + e];
+                    for (int i = 1; i <= 2; ++i)
+                        eg.push_back(std::fma(m.shape_funcs[(size_t)(3 + i) * mNe + e], ny,
+                                              m.shape_funcs[(size_t)i * mNe + e] * nx));
+                    eg.push_back(ny);
+                }
+                for (int j = 0; j < 3; ++j) {
+                    node.push_back(v[j]);
+                    code.push_back((3 * e + j) << 1);
+                    node.push_back(v[(j + 1) % 3]);
+                    code.push_back(((3 * e + j) << 1) | 1);
+                }
+                ebf.push_back((int)bv.size() - d.bitem);
+                int cnt = 0;
+                for (int j = 0; j < 3; ++j) {
+                    if (m.boundary_edges[(size_t)j * mNe + e] != 1) continue;
+                    for (int sh = 0; sh < 2; ++sh) {
+                        bv.push_back(v[(j + sh) % 3]);
+                        const double nbx = m.boundary_edge_normals[(size_t)(4 * j + 2 * sh) * mNe + e];
+                        const double nby = m.boundary_edge_normals[(size_t)(4 * j + 2 * sh + 1) * mNe + e];
+                        for (int i = 1; i <= 2; ++i)
+                            bn.push_back(std::fma(m.shape_funcs[(size_t)(3 + i) * mNe + e], nby,
+                                                  m.shape_funcs[(size_t)i * mNe + e] * nbx));
+                        bn.push_back(nby);
+                        ++cnt;
+                    }
+                }
+                ebc.push_back(cnt);
             }
-            ebc[e] = (int)bv.size() - ebf[e];
+            d.nb = (int)bv.size() - d.bitem;
+            d.state = 4 * mn + 3 * mNe + d.nb;
+            Csr csr = group_events(mn, node, code);
+            cptr.insert(cptr.end(), csr.ptr.begin(), csr.ptr.end());
+            cent.insert(cent.end(), csr.ent.begin(), csr.ent.end());
+            for (int l = 0; l < mn; ++l) {
+                bnode.push_back(m.boundary_nodes[l]);
+                cv.push_back(m.CV_area[l]);
+            }
+            for (int l = 0; l < 2 * mn; ++l) vec.push_back(m.vectors[l]);
+            c->tpl_host.push_back(d);
         }
-        T.nb = (int)bv.size();
-        Csr csr = group_events(mn, node, code);
-        if ((rc = upload(c, ev.data(), ev.size(), &T.ev))) return rc;
-        if ((rc = upload(c, eg.data(), eg.size(), &T.eg))) return rc;
-        if ((rc = upload(c, csr.ptr.data(), csr.ptr.size(), &T.csr_ptr))) return rc;
-        if ((rc = upload(c, csr.ent.data(), csr.ent.size(), &T.csr_ent))) return rc;
-        if ((rc = upload(c, m.boundary_nodes, (size_t)mn, &T.bnode))) return rc;
-        if ((rc = upload(c, m.CV_area, (size_t)mn, &T.cv))) return rc;
-        if ((rc = upload(c, m.vectors, 2 * (size_t)mn, &T.vec))) return rc;
-        if ((rc = upload(c, ebf.data(), ebf.size(), &T.eb_first))) return rc;
-        if ((rc = upload(c, ebc.data(), ebc.size(), &T.eb_count))) return rc;
-        if ((rc = upload(c, bv.data(), bv.size(), &T.b_v))) return rc;
-        if ((rc = upload(c, bn.data(), bn.size(), &T.b_n))) return rc;
+        const TplDesc* dt;
+        if ((rc = upload(c, c->tpl_host.data(), c->tpl_host.size(), &dt))) return rc;
+        S.tpl = dt;
+        if ((rc = upload(c, ev.data(), ev.size(), &S.ev))) return rc;
+        if ((rc = upload(c, eg.data(), eg.size(), &S.eg))) return rc;
+        if ((rc = upload(c, cptr.data(), cptr.size(), &S.csr_ptr))) return rc;
+        if ((rc = upload(c, cent.data(), cent.size(), &S.csr_ent))) return rc;
+        if ((rc = upload(c, bnode.data(), bnode.size(), &S.bnode))) return rc;
+        if ((rc = upload(c, cv.data(), cv.size(), &S.cv))) return rc;
+        if ((rc = upload(c, vec.data(), vec.size(), &S.vec))) return rc;
+        if ((rc = upload(c, ebf.data(), ebf.size(), &S.eb_first))) return rc;
+        if ((rc = upload(c, ebc.data(), ebc.size(), &S.eb_count))) return rc;
+        if ((rc = upload(c, bv.data(), bv.size(), &S.b_v))) return rc;
+        if ((rc = upload(c, bn.data(), bn.size(), &S.b_n))) return rc;
+        if ((rc = upload(c, cell_off.data(), cell_off.size(), &S.cell_off))) return rc;
+        if ((rc = upload(c, c->cell_tpl_host.data(), c->cell_tpl_host.size(), &S.cell_tpl))) return rc;
+        S.cell_par = nullptr;
+        if (batched && ext->cell_soilB) {
+            std::vector<VGPar> par((size_t)Ne);
+            for (int k = 0; k < Ne; ++k) par[k] = make_vg(ext->cell_soilB[k]);
+            const VGPar* dp;
+            if ((rc = upload(c, par.data(), par.size(), &dp))) return rc;
+            S.cell_par = dp;
+        }
     }
     void* p;
     if ((rc = dev_alloc(c, sizeof(double) * 16 * (size_t)Ne, &p))) return rc;
@@ -327,29 +482,18 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
     if ((rc = dev_alloc(c, sizeof(int) * 4, &p))) return rc;
     P.flag = (int*)p;
     CK(cudaMemset(P.flag, 0, sizeof(int) * 4));
-    // launch shape of the cell kernel (TSR_CELL_THREADS overrides: 64..256);
-    // 256 threads keep 32 warps per SM in flight at 4 cells per SM
-    P.micro_block = 256;
+    if ((rc = dev_alloc(c, sizeof(int) * 4 * (size_t)Ne, &p))) return rc;
+    c->d_bundle = (int*)p;
+    CK(cudaDeviceGetAttribute(&c->dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+    CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device));
+    // default launch shape: 256 threads; the smallest shared-memory budget
+    // of at least 48 KB that holds one cell of every template
+    int threads = 256;
     if (const char* e = std::getenv("TSR_CELL_THREADS")) {
         int v = std::atoi(e);
-        if (v >= 64 && v <= 256 && v % 32 == 0) P.micro_block = v;
+        if (v >= 64 && v <= 256 && v % 32 == 0) threads = v;
     }
-    const size_t tab = sizeof(tsr_math_tables);
-    P.micro_smem = tab + sizeof(double) * (4 * (size_t)mn + 3 * (size_t)mNe + (size_t)T.nb + 16);
-    int dev_smem = 0, nsm = 0;
-    CK(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
-    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
-    if (P.micro_smem > (size_t)dev_smem) {
-        set_error("micro mesh too large for one cell in shared memory");
-        return TSR_ERR_ARG;
-    }
-    int occ = 1;
-    rc = tsr::configure_cell_kernels(P, &occ);
-    if (rc) return rc;
-    long long grid = (long long)occ * nsm;
-    P.micro_grid = (int)(grid < Ne ? grid : Ne);
-    if (P.micro_grid < 1) P.micro_grid = 1;
-    return TSR_OK;
+    return tsr::plan_cells(c, threads, 48 * 1024);
 }
 
 int alloc_work(tsr_ctx* c, int max_krylov)
@@ -1026,4 +1170,51 @@ extern "C" void* tsr_pinned_alloc(size_t bytes)
 extern "C" void tsr_pinned_free(void* p)
 {
     if (p) cudaFreeHost(p);
+}
+
+// ---- autotuner of the cell kernel's packing and block size ---------------------
+// Times G on the given state for every (threads, shared-memory budget) pair
+// that fits and keeps the fastest plan.  Plans differ only in how cells are
+// packed into CTAs; every plan gives the same bits.
+
+extern "C" int tsr_autotune(tsr_ctx* c, const double* u_host, int reps, double* best_ms,
+                            int* best_threads, int* best_budget)
+{
+    if (!c || !u_host) return TSR_ERR_ARG;
+    if (reps < 1) reps = 3;
+    CK(cudaMemcpyAsync(c->d_x, u_host, sizeof(double) * (size_t)c->N, cudaMemcpyHostToDevice, c->stream));
+    const int thr[] = {128, 256};
+    const int bud[] = {48 * 1024, 64 * 1024, 96 * 1024, 144 * 1024, 200 * 1024};
+    double best = 1e30;
+    int bt = c->tuned_threads, bb = c->tuned_budget;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    for (int T : thr)
+        for (int B : bud) {
+            if (B > c->dev_smem) continue;
+            if (tsr::plan_cells(c, T, B) != TSR_OK) continue;
+            launch_g(c->P, 0, c->d_x, nullptr, nullptr, 0.0, 0.0, c->d_y, c->stream);   // warm
+            CK(cudaEventRecord(e0, c->stream));
+            for (int r = 0; r < reps; ++r)
+                launch_g(c->P, 0, c->d_x, nullptr, nullptr, 0.0, 0.0, c->d_y, c->stream);
+            CK(cudaEventRecord(e1, c->stream));
+            CK(cudaEventSynchronize(e1));
+            CK(cudaGetLastError());
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms / reps < best) {
+                best = ms / reps;
+                bt = T;
+                bb = B;
+            }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    int rc = tsr::plan_cells(c, bt, bb);
+    if (rc) return rc;
+    if (best_ms) *best_ms = best;
+    if (best_threads) *best_threads = bt;
+    if (best_budget) *best_budget = bb;
+    return TSR_OK;
 }

@@ -14,22 +14,39 @@ struct VGPar {
     double dth, coefC, mh;
 };
 
-// Micro-cell template: the reference's one shared micro mesh
-// (include/user_data.h:4) re-laid out for the cell kernel.
-struct MicroTpl {
-    int mn, mNe, nb;
+// Micro-cell templates: the reference's one shared micro mesh
+// (include/user_data.h:4), or several in the batched form, re-laid out for
+// the cell kernel and concatenated; TplDesc holds each template's sizes and
+// its offsets into the concatenated arrays.
+struct TplDesc {
+    int mn, mNe, nb, state;      // nodes, elements, boundary items, shared doubles per cell
+    int ev, eg, csr_ptr, csr_ent, node, bitem;   // offsets (elements, nodes, items)
+};
+
+struct MicroSet {
+    int ntpl;
+    int n_bundles;
+    int maxc;                    // largest bundle (cells)
     int pad;
-    const int* ev;          // [3*mNe]  vertices of element e at 3e+j
-    const double* eg;       // [9*mNe] per face j of element e: D1, D2, ny (see tsr_ctx.cu)
-    const int* csr_ptr;     // [mn+1]
-    const int* csr_ent;     // (3e+j)<<1 | (1 if subtracted)
-    const int* bnode;       // [mn]
-    const double* cv;       // [mn]
-    const double* vec;      // [2*mn] x block then y block
-    const int* eb_first;    // [mNe] first boundary item of element e
-    const int* eb_count;    // [mNe]
-    const int* b_v;         // [nb] node of item
-    const double* b_n;      // [3*nb] per item: D1, D2 and ny of its outward normal
+    const TplDesc* tpl;          // [ntpl]
+    const int* ev;               // 3 per element: vertices
+    const double* eg;            // 9 per element: per face j D1, D2, ny
+    const int* csr_ptr;          // mn+1 per template
+    const int* csr_ent;          // (3e+j)<<1 | (1 if subtracted)
+    const int* bnode;            // per node: 1 on the inclusion boundary
+    const double* cv;            // per node: CV area
+    const double* vec;           // 2 per node (x then y, per template block)
+    const int* eb_first;         // per element: first boundary item (template-local)
+    const int* eb_count;         // per element
+    const int* b_v;              // per item: node (template-local)
+    const double* b_n;           // 3 per item: D1, D2, ny of the outward normal
+    const long long* cell_off;   // [Ne] first unknown of cell k
+    const int* cell_tpl;         // [Ne]
+    const struct VGPar* cell_par;   // [Ne] or nullptr (all pB)
+    const int* bundle_tpl;       // [n_bundles]
+    const int* bundle_first;     // [n_bundles] index into bundle_cells
+    const int* bundle_count;     // [n_bundles]
+    const int* bundle_cells;     // cell ids, grouped by bundle
 };
 
 // Macro mesh in the reference layout plus derived arrays.
@@ -60,13 +77,14 @@ struct MacroDev {
 
 struct Problem {
     MacroDev M;
-    MicroTpl m;
+    MicroSet m;
     VGPar pA, pB;
     const double* cell_scale;   // [Ne] or nullptr
     int kface;
     int micro_block;            // threads per cell CTA
     size_t micro_smem;          // dynamic shared memory per cell CTA
     int micro_grid;             // persistent grid of the cell kernel
+    int misc_slots;             // per-cell scratch slots reserved in shared memory
     double* contrib;            // [16*Ne] macro contributions per element
     int* flag;                  // device word: bit 0 non-finite G
     long long N;

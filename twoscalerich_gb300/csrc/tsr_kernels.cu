@@ -225,8 +225,15 @@ __device__ __forceinline__ void macro_element_terms(const Problem& P, int k, con
 }
 
 // ---- the micro-cell kernel ----------------------------------------------
-// Dynamic shared memory: tables | h[mn] | Kh[mn] | Cd[mn] | den[mn] |
-// F[3 mNe] | items[nb] | misc[16] (interpolant coefficients, vertex heads).
+// A persistent CTA walks bundles: groups of cells that share one template
+// (one cell per bundle for large templates, many for small ones, as packed
+// by the host-side autotuner).  For a bundle of nc cells with mn nodes and
+// mNe elements each, dynamic shared memory holds
+//   tables | misc [slots x 16] | cell ids / offsets [slots] |
+//   h[nc mn] | Kh[nc mn] | Cd[nc mn] | den[nc mn] | F[nc 3 mNe] | items[nc nb]
+// and the threads sweep the bundle's flattened node and element index
+// spaces.  Every cell still follows the single-cell operation sequence (the
+// same as the host oracle), so packing changes speed, never bits.
 template <int MODE>
 __global__ void __launch_bounds__(256) k_cells(Problem P, const double* __restrict__ u,
                                                const double* __restrict__ v,
@@ -235,125 +242,160 @@ __global__ void __launch_bounds__(256) k_cells(Problem P, const double* __restri
 {
     extern __shared__ double sm[];
     tsr_math_tables* T = reinterpret_cast<tsr_math_tables*>(sm);
-    const int mn = P.m.mn, mNe = P.m.mNe, nb = P.m.nb;
-    double* h = sm + kTabDoubles;
-    double* Kh = h + mn;
-    double* Cd = Kh + mn;
-    double* den = Cd + mn;
-    double* F = den + mn;
-    double* items = F + 3 * mNe;
-    double* misc = items + nb;
+    double* misc = sm + kTabDoubles;                         // 16 per cell slot
+    long long* coff = reinterpret_cast<long long*>(misc + 16 * P.misc_slots);
+    int* ck = reinterpret_cast<int*>(coff + P.misc_slots);
+    double* st = reinterpret_cast<double*>(ck + 2 * P.misc_slots);
     const int tid = threadIdx.x, bs = blockDim.x;
-    const int lane = tid & 31;
+    const int lane = tid & 31, warp = tid >> 5, nwarps = bs >> 5;
     const MacroDev& M = P.M;
+    const MicroSet& S = P.m;
     const int nv = M.nv, Ne = M.Ne;
     const bool exch = (M.model_type == 3);
     load_tables(T);
     int bad = 0;
-    for (int k = blockIdx.x; k < Ne; k += gridDim.x) {
+    for (int b = blockIdx.x; b < S.n_bundles; b += gridDim.x) {
         __syncthreads();
-        if (tid < 32) {
-            // vertex heads, then interpolant coefficients of element k
-            if (lane < nv) misc[8 + lane] = state_at<MODE>(u, v, eps, M.elements[(long long)lane * Ne + k]);
+        const int t = S.bundle_tpl[b], first = S.bundle_first[b], nc = S.bundle_count[b];
+        const TplDesc D = S.tpl[t];
+        const int mn = D.mn, mNe = D.mNe, nb = D.nb;
+        double* h = st;
+        double* Kh = h + nc * mn;
+        double* Cd = Kh + nc * mn;
+        double* den = Cd + nc * mn;
+        double* F = den + nc * mn;
+        double* items = F + nc * 3 * mNe;
+        const int* ev = S.ev + D.ev;
+        const double* eg = S.eg + D.eg;
+        const int* cptr = S.csr_ptr + D.csr_ptr;
+        const int* cent = S.csr_ent + D.csr_ent;
+        const int* bnode = S.bnode + D.node;
+        const double* cvm = S.cv + D.node;
+        const double* vec = S.vec + 2 * D.node;
+        const int* ebf = S.eb_first + D.ev / 3;
+        const int* ebc = S.eb_count + D.ev / 3;
+        const int* bvv = S.b_v + D.bitem;
+        const double* bnn = S.b_n + 3 * (long long)D.bitem;
+        // per cell: id, first unknown, vertex heads and interpolant coefficients
+        for (int c = warp; c < nc; c += nwarps) {
+            const int k = S.bundle_cells[first + c];
+            double* mc = misc + 16 * c;
+            if (lane == 0) {
+                ck[c] = k;
+                coff[c] = S.cell_off[k];
+                mc[4] = P.cell_scale ? P.cell_scale[k] : 1.0;
+                mc[5] = M.cent[k];
+                mc[6] = M.cent[Ne + k];
+            }
+            if (lane < nv) mc[8 + lane] = state_at<MODE>(u, v, eps, M.elements[(long long)lane * Ne + k]);
             __syncwarp();
             if (lane < nv) {
                 const int m = lane;
-                double a = M.sf[(long long)(m * nv + 0) * Ne + k] * misc[8];
+                double a = M.sf[(long long)(m * nv + 0) * Ne + k] * mc[8];
                 for (int i = 1; i < nv; ++i)
-                    a = fma(M.sf[(long long)(m * nv + i) * Ne + k], misc[8 + i], a);
-                misc[m] = a;
+                    a = fma(M.sf[(long long)(m * nv + i) * Ne + k], mc[8 + i], a);
+                mc[m] = a;
             }
         }
         __syncthreads();
-        const long long off = (long long)M.Mn + (long long)k * mn;
-        const double s = P.cell_scale ? P.cell_scale[k] : 1.0;
-        const double s2 = s * s;
-        const double cx = M.cent[k], cy = M.cent[Ne + k];
         // nodes: head, conductivity, storage
-        for (int l = tid; l < mn; l += bs) {
-            const bool bnd = P.m.bnode[l] != 0;
+        for (int idx = tid; idx < nc * mn; idx += bs) {
+            const int c = idx / mn, l = idx - c * mn;
+            const double* mc = misc + 16 * c;
+            const double s = mc[4];
+            const VGPar& pB = S.cell_par ? S.cell_par[ck[c]] : P.pB;
+            const bool bnd = bnode[l] != 0;
             double hl;
             if (bnd) {
-                double px = cx, py = cy;
+                double px = mc[5], py = mc[6];
                 if (M.model_type != 1) {
-                    px = fma(s, P.m.vec[l], cx);
-                    py = fma(s, P.m.vec[mn + l], cy);
+                    px = fma(s, vec[l], mc[5]);
+                    py = fma(s, vec[mn + l], mc[6]);
                 }
-                hl = interp_at(nv, misc, px, py);
+                hl = interp_at(nv, mc, px, py);
             } else {
-                hl = state_at<MODE>(u, v, eps, off + l);
+                hl = state_at<MODE>(u, v, eps, coff[c] + l);
             }
-            h[l] = hl;
+            h[idx] = hl;
             double K, Cn, Cdl;
-            vg_full(hl, P.pB, T, K, Cn, Cdl);
-            Kh[l] = 0.5 * K;
-            Cd[l] = Cdl;
-            den[l] = fma(M.Ss, Cdl, Cn) * (P.m.cv[l] * s2);
+            vg_full(hl, pB, T, K, Cn, Cdl);
+            Kh[idx] = 0.5 * K;
+            Cd[idx] = Cdl;
+            den[idx] = fma(M.Ss, Cdl, Cn) * (cvm[l] * (s * s));
         }
         __syncthreads();
         // elements: SCV face fluxes and inclusion-boundary exchange items
-        for (int e = tid; e < mNe; e += bs) {
-            const int v0 = P.m.ev[3 * e], v1 = P.m.ev[3 * e + 1], v2 = P.m.ev[3 * e + 2];
-            const double* G = P.m.eg + 9 * (long long)e;   // per face: D1, D2, ny
-            const double h0 = h[v0];
-            const double d1 = h[v1] - h0, d2 = h[v2] - h0;
+        for (int idx = tid; idx < nc * mNe; idx += bs) {
+            const int c = idx / mNe, e = idx - c * mNe;
+            const double s = misc[16 * c + 4];
+            const double* hc = h + c * mn;
+            const double* Khc = Kh + c * mn;
+            const int v0 = ev[3 * e], v1 = ev[3 * e + 1], v2 = ev[3 * e + 2];
+            const double* G = eg + 9 * (long long)e;   // per face: D1, D2, ny
+            const double h0 = hc[v0];
+            const double d1 = hc[v1] - h0, d2 = hc[v2] - h0;
             const int vv[3] = {v0, v1, v2};
+            double* Fc = F + (long long)c * 3 * mNe;
 #pragma unroll
             for (int j = 0; j < 3; ++j) {
-                const int a = vv[j], b = vv[(j + 1) % 3];
+                const int a = vv[j], bb = vv[(j + 1) % 3];
                 double dot = fma(G[3 * j + 1], d2, fma(G[3 * j], d1, s * G[3 * j + 2]));
                 double Kf;
                 if (P.kface == 1)
-                    Kf = (dot > 0.0) ? (2.0 * Kh[b]) : (2.0 * Kh[a]);
+                    Kf = (dot > 0.0) ? (2.0 * Khc[bb]) : (2.0 * Khc[a]);
                 else
-                    Kf = Kh[a] + Kh[b];
-                F[3 * e + j] = Kf * dot;
+                    Kf = Khc[a] + Khc[bb];
+                Fc[3 * e + j] = Kf * dot;
             }
             if (exch) {
-                const int c = P.m.eb_count[e];
-                if (c > 0) {
-                    const int f0 = P.m.eb_first[e];
-                    for (int q = 0; q < c; ++q) {
-                        const int it = f0 + q;
-                        const double* B = P.m.b_n + 3 * (long long)it;   // Db1, Db2, nby
-                        items[it] = (2.0 * Kh[P.m.b_v[it]]) * fma(B[1], d2, fma(B[0], d1, s * B[2]));
+                const int cnt = ebc[e];
+                if (cnt > 0) {
+                    const int f0 = ebf[e];
+                    double* it = items + c * nb;
+                    for (int q = 0; q < cnt; ++q) {
+                        const double* B = bnn + 3 * (long long)(f0 + q);   // Db1, Db2, nby
+                        it[f0 + q] = (2.0 * Khc[bvv[f0 + q]]) * fma(B[1], d2, fma(B[0], d1, s * B[2]));
                     }
                 }
             }
         }
         __syncthreads();
         // nodes: gather face fluxes in the fixed order, divide by storage
-        for (int l = tid; l < mn; l += bs) {
+        for (int idx = tid; idx < nc * mn; idx += bs) {
+            const int c = idx / mn, l = idx - c * mn;
             double g;
-            if (P.m.bnode[l]) {
+            if (bnode[l]) {
                 g = 0.0;
             } else {
+                const double* Fc = F + (long long)c * 3 * mNe;
                 double acc = 0.0;
-                const int p1 = P.m.csr_ptr[l + 1];
-                for (int p = P.m.csr_ptr[l]; p < p1; ++p) {
-                    const int ent = P.m.csr_ent[p];
-                    const double f = F[ent >> 1];
+                const int p1 = cptr[l + 1];
+                for (int p = cptr[l]; p < p1; ++p) {
+                    const int ent = cent[p];
+                    const double f = Fc[ent >> 1];
                     acc = (ent & 1) ? (acc - f) : (acc + f);
                 }
-                g = (acc * Cd[l]) / den[l];
+                g = (acc * Cd[idx]) / den[idx];
             }
             if (!finite_d(g)) bad = 1;
+            const long long o = coff[c] + l;
             if (MODE == 0)
-                out[off + l] = g;
+                out[o] = g;
             else
-                out[off + l] = (g - g0[off + l]) * inv_eps;
+                out[o] = (g - g0[o]) * inv_eps;
         }
-        // exchange flux and the macro element terms (warp 0)
-        if (tid < 32) {
+        // exchange flux and the macro element terms: one warp per cell
+        for (int c = warp; c < nc; c += nwarps) {
             double Q = 0.0;
             if (exch) {
+                const double* it = items + c * nb;
                 double p = 0.0;
-                for (int i = lane; i < nb; i += 32) p = p + items[i];
+                for (int i = lane; i < nb; i += 32) p = p + it[i];
 #pragma unroll
                 for (int d = 16; d >= 1; d >>= 1) p = p + __shfl_xor_sync(0xffffffffu, p, d);
                 Q = p;
             }
-            macro_element_terms(P, k, misc, Q, T, lane);
+            macro_element_terms(P, ck[c], misc + 16 * c, Q, T, lane);
         }
     }
     if (bad) atomicOr(P.flag, 1);
@@ -663,10 +705,17 @@ __global__ void k_water_macro(Problem P, const double* __restrict__ u, double* _
 __global__ void k_water_cells(Problem P, const double* __restrict__ u, double* __restrict__ terms)
 {
     const MacroDev& M = P.M;
+    const MicroSet& S = P.m;
     const int lane = threadIdx.x & 31;
     const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (k >= M.Ne) return;
-    const int nv = M.nv, Ne = M.Ne, mn = P.m.mn;
+    const int nv = M.nv, Ne = M.Ne;
+    const TplDesc D = S.tpl[S.cell_tpl[k]];
+    const int mn = D.mn;
+    const int* bnode = S.bnode + D.node;
+    const double* cvm = S.cv + D.node;
+    const double* vec = S.vec + 2 * D.node;
+    const VGPar& pB = S.cell_par ? S.cell_par[k] : P.pB;
     double al[4];
     for (int m = 0; m < nv; ++m) {
         double a = M.sf[(long long)(m * nv) * Ne + k] * u[M.elements[k]];
@@ -676,22 +725,22 @@ __global__ void k_water_cells(Problem P, const double* __restrict__ u, double* _
     }
     const double s = P.cell_scale ? P.cell_scale[k] : 1.0;
     const double cx = M.cent[k], cy = M.cent[Ne + k];
-    const long long off = (long long)M.Mn + (long long)k * mn;
+    const long long off = S.cell_off[k];
     double p = 0.0;
     for (int l = lane; l < mn; l += 32) {
         double hl;
-        if (P.m.bnode[l]) {
+        if (bnode[l]) {
             double px = cx, py = cy;
             if (M.model_type != 1) {
-                px = fma(s, P.m.vec[l], cx);
-                py = fma(s, P.m.vec[mn + l], cy);
+                px = fma(s, vec[l], cx);
+                py = fma(s, vec[mn + l], cy);
             }
             hl = interp_at(nv, al, px, py);
         } else {
             hl = u[off + l];
         }
-        double Se = vg_se(hl, P.pB, &d_tables);
-        p = p + fma(P.pB.dth, Se, P.pB.thr) * P.m.cv[l];
+        double Se = vg_se(hl, pB, &d_tables);
+        p = p + fma(pB.dth, Se, pB.thr) * cvm[l];
     }
 #pragma unroll
     for (int d = 16; d >= 1; d >>= 1) p = p + __shfl_xor_sync(0xffffffffu, p, d);

@@ -165,3 +165,19 @@ def read_mesh(path, micro=False):
     ne = int(nxt())
     el = np.array([int(nxt()) for _ in range(nv * ne)], dtype=np.int64) - 1
     return Mesh(nv, xy, el, bed.ravel(), cell=cell)
+
+
+def micro_disk_inclusion(n, cell=1.0, diameter=0.5):
+    """A disk inclusion of diameter `diameter`*cell centred in the cell,
+    meshed by an n x n grid mapped onto the disk (elliptical grid mapping
+    (a, b) -> (a sqrt(1 - b^2/2), b sqrt(1 - a^2/2)), orientation
+    preserving); the square's boundary maps onto the circle."""
+    s = np.linspace(-1.0, 1.0, n)
+    A, B = np.meshgrid(s, s)                     # node id = j*n + i
+    X = A * np.sqrt(1.0 - B * B / 2.0)
+    Y = B * np.sqrt(1.0 - A * A / 2.0)
+    r = 0.5 * diameter * cell
+    xy = np.concatenate([0.5 * cell + r * X.ravel(), 0.5 * cell + r * Y.ravel()])
+    elems = _grid_tris(n, n)
+    bed = _grid_boundary(n, n, xy, lambda *a: -1)
+    return Mesh(3, xy, elems, bed, cell=(cell, cell))

@@ -53,7 +53,11 @@ class Problem:
 
     def __init__(self, macro, micro, keff_rows, epsA, soilA, soilB, *, macro_bc,
                  model_type=3, boundary_flux=0.0, dirichlet_h=0.0, specific_storage=1e-6,
-                 kface=0, cell_scale=None, logh_first=None, logr=None, name=""):
+                 kface=0, cell_scale=None, logh_first=None, logr=None, name="",
+                 templates=None, cell_template=None, cell_soilB=None):
+        """micro: the micro mesh of every cell; or, for the batched form,
+        templates (list of micro meshes) with cell_template[k] naming the
+        template of cell k and optional per-cell material B (list of dicts)."""
         lib = capi.load()
         self.name = name
         self.macro = capi.MacroMesh()
@@ -62,6 +66,16 @@ class Problem:
         check(lib.tsr_macro_mesh_build(macro.nv, macro.n_nodes, ptr(macro.xy), macro.n_elems,
                                        ptr(macro.elems), macro.bedges.size // 3, ptr(macro.bedges),
                                        ptr(self._bc), C.byref(self.macro)), "tsr_macro_mesh_build")
+        if templates is not None:
+            micro = templates[0]
+        self._tpl = None
+        if templates is not None:
+            self._tpl = (capi.MicroMesh * len(templates))()
+            for i, t in enumerate(templates):
+                check(lib.tsr_micro_mesh_build(t.cell[0], t.cell[1], t.nv, t.n_nodes, ptr(t.xy),
+                                               t.n_elems, ptr(t.elems), t.bedges.size // 3,
+                                               ptr(t.bedges), C.byref(self._tpl[i])),
+                      "tsr_micro_mesh_build")
         check(lib.tsr_micro_mesh_build(micro.cell[0], micro.cell[1], micro.nv, micro.n_nodes,
                                        ptr(micro.xy), micro.n_elems, ptr(micro.elems),
                                        micro.bedges.size // 3, ptr(micro.bedges),
@@ -90,14 +104,30 @@ class Problem:
         self.Mn = self.macro.no_nodes
         self.Ne = self.macro.no_elements
         self.mn = self.micro.no_nodes
-        self.N = self.Mn + self.Ne * self.mn
-        self.ud.N = self.N
         self._scale = None if cell_scale is None else np.ascontiguousarray(cell_scale, np.float64)
         self.ext = capi.ModelExt()
         self.ext.dirichlet_h = dirichlet_h
         self.ext.specific_storage = specific_storage
         self.ext.kface_mode = kface
         self.ext.cell_scale = ptr(self._scale)
+        if templates is not None:
+            self.cell_template = np.ascontiguousarray(cell_template, dtype=np.int32)
+            mns = np.array([t.no_nodes for t in self._tpl], dtype=np.int64)
+            self.cell_nodes = mns[self.cell_template]
+            self.cell_off = self.Mn + np.concatenate([[0], np.cumsum(self.cell_nodes)[:-1]])
+            self.N = int(self.Mn + self.cell_nodes.sum())
+            self.ext.n_templates = len(templates)
+            self.ext.templates = C.cast(self._tpl, C.POINTER(capi.MicroMesh))
+            self.ext.cell_template = ptr(self.cell_template)
+            if cell_soilB is not None:
+                self._soils = (capi.Soil * self.Ne)(*[make_soil(**s) for s in cell_soilB])
+                self.ext.cell_soilB = C.cast(self._soils, C.POINTER(capi.Soil))
+        else:
+            self.cell_template = None
+            self.cell_nodes = np.full(self.Ne, self.mn, dtype=np.int64)
+            self.cell_off = self.Mn + self.mn * np.arange(self.Ne, dtype=np.int64)
+            self.N = self.Mn + self.Ne * self.mn
+        self.ud.N = self.N
         self.dirichlet_h = dirichlet_h
         bce = capi.as_array(self.macro.boundary_condition_edges, macro.nv * self.Ne, np.int32)
         el = capi.as_array(self.macro.elements, macro.nv * self.Ne, np.int32)
@@ -129,6 +159,11 @@ class Problem:
             lib.tsr_macro_mesh_free(C.byref(self.macro))
         if self.micro.elements:
             lib.tsr_micro_mesh_free(C.byref(self.micro))
+        if self._tpl is not None:
+            for t in self._tpl:
+                if t.elements:
+                    lib.tsr_micro_mesh_free(C.byref(t))
+            self._tpl = None
 
     def __del__(self):
         try:
@@ -182,6 +217,46 @@ def config2(n_macro=201, n_micro=21, seed=GENERATOR_SEED, eval_seed=EVAL_SEED):
     return p
 
 
+MICRO_SIDES = (5, 9, 15, 21, 31, 41)
+MICRO_SIDE_P = (0.30, 0.25, 0.20, 0.12, 0.08, 0.05)
+
+
+def config3(n_macro=151, seed=GENERATOR_SEED, eval_seed=EVAL_SEED):
+    """Batched form with uneven micro meshes: n_macro^2 macro nodes; per cell
+    a micro mesh side from {5,9,15,21,31,41} (p = .30,.25,.20,.12,.08,.05), a
+    square or disk inclusion (p = 0.5) of size U(0.2, 0.8) of the cell, and
+    material B perturbed by lognormal factors (sigma 0.2 on alpha and Ks,
+    0.05 on n).  Dirichlet top strip, EXPREM as config1."""
+    h = 1.0 / (n_macro - 1)
+    macro = meshgen.macro_unit_square(n_macro, segment=(0.25, 0.75))
+    templates = []
+    for n in MICRO_SIDES:
+        templates.append(meshgen.micro_square_inclusion(n, cell=h, side=0.5))
+        templates.append(meshgen.micro_disk_inclusion(n, cell=h, diameter=0.5))
+    Ne = 2 * (n_macro - 1) ** 2
+    rng = np.random.default_rng(seed)
+    side = rng.choice(len(MICRO_SIDES), size=Ne, p=MICRO_SIDE_P)
+    disk = rng.random(Ne) < 0.5
+    size = rng.uniform(0.2, 0.8, Ne)
+    tpl = (2 * side + disk).astype(np.int32)
+    scale = size / 0.5
+    fa = rng.lognormal(0.0, 0.2, Ne)
+    fk = rng.lognormal(0.0, 0.2, Ne)
+    fn = rng.lognormal(0.0, 0.05, Ne)
+    soils = [dict(SOIL_B, alpha=SOIL_B["alpha"] * a, Ksat=SOIL_B["Ksat"] * k,
+                  n=max(1.05, SOIL_B["n"] * n_)) for a, k, n_ in zip(fa, fk, fn)]
+    frac = np.where(disk, np.pi * size ** 2 / 4.0, size ** 2)
+    p = Problem(macro, None, constant_keff_rows(0.02), 1.0 - frac.mean(), SOIL_A, SOIL_B,
+                macro_bc=[5, 2, 2, 2, 2], model_type=3, dirichlet_h=-0.1, cell_scale=scale,
+                templates=templates, cell_template=tpl, cell_soilB=soils,
+                name="config3_%d" % n_macro)
+    p.options = default_options(AbsTol=1e-6, RelTol=1e-6, MaxKrylov=30)
+    p.tend = 1.0
+    p.tspan = np.concatenate([[10.0], np.linspace(0.1, 1.0, 10)])
+    p.u0 = p.initial_state(-5.0, noise=0.1, seed=eval_seed)
+    return p
+
+
 def fixture10(boundary_flux=0.05, jitter=0.25, seed=GENERATOR_SEED):
     """The shape of the reference's test scenario: 10x10 quadrilaterals,
     influx segment x in [0, 0.4] on the top (BC 1), free drainage dh/dx = 0
@@ -230,6 +305,13 @@ class Context:
         w = C.c_double()
         check(self.lib.tsr_water_content(self.h, ptr(u), C.byref(w)), "tsr_water_content")
         return w.value
+
+    def autotune(self, u, reps=3):
+        """Pick the cell kernel's block size and packing by timing G at u."""
+        ms, thr, bud = C.c_double(), C.c_int(), C.c_int()
+        check(self.lib.tsr_autotune(self.h, ptr(u), reps, C.byref(ms), C.byref(thr), C.byref(bud)),
+              "tsr_autotune")
+        return ms.value, thr.value, bud.value
 
     def dot(self, x, y):
         r = C.c_double()
