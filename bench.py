@@ -150,18 +150,38 @@ def allsum(dist, x):
 
 def make_problem(args):
     from twoscalerich_gb300 import problem as P
-    p = P.config2(n_macro=args.n_macro, n_micro=args.n_micro)
+    if args.config == 3:
+        p = P.config3(n_macro=args.n_macro)
+    else:
+        p = P.config2(n_macro=args.n_macro, n_micro=args.n_micro)
     p.options.MaxKrylov = args.max_krylov
     return p
 
 
+def l2_statement(args, N):
+    """No L2 flush: each step streams the Krylov basis and state vectors,
+    a working set far above the 129 MB L2."""
+    vec = N * 8 / 1e6
+    return ("inputs larger than L2: one unknown vector is %.0f MB; an EXPREM step streams the "
+            "Krylov basis and 5 state vectors, %.0f MB at Krylov dimension 7 (L2 129 MB)"
+            % (vec, vec * (7 + 1 + 5)))
+
+
 def workload(args, N):
+    if args.config == 3:
+        return {"workload": "two-scale Richards, batched uneven micro meshes, EXPREM steps",
+                "macro_nodes": "%dx%d" % (args.n_macro, args.n_macro),
+                "micro_nodes_per_cell": "5..41 per side (p .30/.25/.20/.12/.08/.05), square or disk",
+                "cells": 2 * (args.n_macro - 1) ** 2, "unknowns": N,
+                "max_krylov": args.max_krylov, "tol": 1e-6,
+                "inputs_vs_l2": l2_statement(args, N),
+                "parallelism": "replicas" if WORLD > 1 else "1 GPU", "packing": "autotuned"}
     return {"workload": "two-scale Richards, plain method, EXPREM steps",
             "macro_nodes": "%dx%d" % (args.n_macro, args.n_macro),
             "micro_nodes_per_cell": "%dx%d" % (args.n_micro, args.n_micro),
             "cells": 2 * (args.n_macro - 1) ** 2, "unknowns": N, "max_krylov": args.max_krylov,
-            "tol": 1e-6, "inputs_vs_l2": "inputs larger than L2 (N x 8 B = %.0f MB > 129 MB)"
-            % (N * 8 / 1e6), "parallelism": "replicas" if WORLD > 1 else "1 GPU"}
+            "tol": 1e-6, "inputs_vs_l2": l2_statement(args, N),
+            "parallelism": "replicas" if WORLD > 1 else "1 GPU"}
 
 
 def cpu_oracle_rate(p, n_evals, threads):
@@ -220,6 +240,7 @@ def run_ours(args):
     N = p.N
     ctx = P.Context(p, max_krylov=p.options.MaxKrylov)
     h = ctx.h
+    tuned = ctx.autotune(p.u0, reps=2)     # packing and block size of the cell kernel
     fp64_peak = C.c_double()
     capi.check(lib.tsr_fp64_peak(C.byref(fp64_peak)), "tsr_fp64_peak")
     opts = p.options
@@ -273,7 +294,7 @@ def run_ours(args):
     gs_gbs = sbytes.value / max(sms.value * 1e-3, 1e-30) / 1e9
     # FP64 instructions per G from the instruction counts of the cell and
     # macro-node kernels (ncu, per unknown) -- see the kernel profiles
-    fp64_per_unknown = FP64_OPS_PER_UNKNOWN.get(args.n_micro)
+    fp64_per_unknown = FP64_OPS_PER_UNKNOWN.get(args.n_micro) if args.config == 2 else None
     fp64 = None
     if fp64_per_unknown:
         ach = fp64_per_unknown * N / (g_avg_ms * 1e-3)
@@ -319,7 +340,7 @@ def run_ours(args):
                "sample": "%d G evaluations of the full workload by the oracle's OpenMP "
                          "Gfunc_parallel form with C-library log/exp (%.1f s)"
                          % (args.cpu_evals, el)}
-    traffic = G_TRAFFIC_PER_UNKNOWN.get(args.n_micro)
+    traffic = G_TRAFFIC_PER_UNKNOWN.get(args.n_micro) if args.config == 2 else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": WORLD, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_max / max(args.steps, 1),
@@ -344,6 +365,8 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * N,
                 "d2h_bytes_per_step": 8 * N},
         "gpu_launches": int(launches),
+        "autotuned": None if tuned is None else {"g_ms": tuned[0], "threads": tuned[1],
+                                                 "smem_budget": tuned[2]},
         "cpu_baseline": cpu,
     }
     if RANK == 0:
@@ -372,8 +395,14 @@ def main():
     ap.add_argument("--n-micro", type=int, default=21)
     ap.add_argument("--cpu-evals", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--max-krylov", type=int, default=40)
+    ap.add_argument("--max-krylov", type=int, default=None)
+    ap.add_argument("--config", type=int, default=2, choices=[2, 3],
+                    help="2: 201x201 x 21x21 plain method; 3: 151x151 batched uneven cells")
     args = ap.parse_args()
+    if args.config == 3 and args.n_macro == 201:
+        args.n_macro = 151
+    if args.max_krylov is None:
+        args.max_krylov = 30 if args.config == 3 else 40
     if args.impl == "reference":
         run_reference(args)
     else:

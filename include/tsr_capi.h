@@ -185,6 +185,10 @@ int tsr_autotune(tsr_ctx* ctx, const double* u_host, int reps, double* best_ms,
 int tsr_profile(tsr_ctx* ctx, int enable);
 int tsr_profile_read(tsr_ctx* ctx, int category, double* ms, long long* count, double* bytes);
 
+/* Replay each Arnoldi step of EXPREM from a captured CUDA graph (1, the
+ * default) or launch its kernels one by one (0).  Same results either way. */
+int tsr_set_graphs(tsr_ctx* ctx, int enable);
+
 /* Number of kernels the library has launched since it was loaded. */
 unsigned long long tsr_kernel_launches(void);
 

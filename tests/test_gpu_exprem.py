@@ -83,6 +83,25 @@ def test_device_resident_stepping_matches_host_stepping():
     assert st.FuncEvals == sth.FuncEvals
 
 
+def test_graph_replay_equals_direct_launches():
+    """Arnoldi steps replayed from captured CUDA graphs give the same
+    trajectory as launching their kernels one by one."""
+    p = P.config2(n_macro=21, n_micro=9)
+    p.tend = 0.1
+    p.tspan = np.array([1.0, 0.1])
+    lib = capi.load()
+    runs = []
+    for graphs in (0, 1):
+        ctx = P.Context(p)
+        capi.check(lib.tsr_set_graphs(ctx.h, graphs), "graphs")
+        launches0 = lib.tsr_kernel_launches()
+        runs.append(P.run_to_end(ctx.exprem_step, p) + (lib.tsr_kernel_launches() - launches0,))
+    (ua, sa, sta, la, na), (ub, sb, stb, lb, nb) = runs
+    assert np.array_equal(ua, ub) and np.array_equal(sa, sb) and la == lb
+    assert sta.FuncEvals == stb.FuncEvals
+    assert na == nb            # replays count the kernels they contain
+
+
 def test_dropin_gfunc_signature_path():
     """tsr_gfunc_gpu is what the C++ Gfunc_gpu(g, u, user_data) calls."""
     p = P.config1()

@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <algorithm>
+#include <array>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -32,7 +33,7 @@ constexpr double kKrylovTol = 0.1;   // Krylov error accepted as a fraction of t
 constexpr int kMaxKrylovCap = 512;
 
 // device scalar slots after the Hessenberg block
-enum { S_HSQ = 0, S_SV, S_ERR, S_DOT, S_BETA2, S_NU2, S_WATER, S_IH, S_COUNT = 16 };
+enum { S_HSQ = 0, S_SV, S_ERR, S_DOT, S_BETA2, S_NU2, S_WATER, S_IH, S_EPS, S_IEPS, S_COUNT = 16 };
 
 }  // namespace
 
@@ -77,6 +78,16 @@ struct tsr_ctx {
     int* d_bundle = nullptr;     // 3 * Ne ints (tpl, first, count) + Ne cell ids
     int nsm = 0, dev_smem = 0;
     int tuned_threads = 0, tuned_budget = 0;
+    // finite-difference step {eps, 1/eps}, staged through pinned memory
+    double* h_eps = nullptr;
+    // one captured graph per Arnoldi index j and state-buffer parity, with
+    // event nodes timing its Jv and its Gram-Schmidt block
+    bool use_graphs = true;
+    double* u_base = nullptr;
+    std::vector<cudaGraphExec_t> graphs[2];
+    std::vector<std::array<cudaEvent_t, 4>> graph_ev[2];
+    double prof_acc_ms[2] = {0.0, 0.0}, prof_acc_bytes[2] = {0.0, 0.0};
+    long long prof_acc_n[2] = {0, 0};
 };
 
 namespace {
@@ -486,12 +497,13 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
     c->d_bundle = (int*)p;
     CK(cudaDeviceGetAttribute(&c->dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
     CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device));
-    // default launch shape: 256 threads; the smallest shared-memory budget
+    // default launch shape: 256 threads (TSR_CELL_THREADS overrides, 64..1024);
+    // the smallest shared-memory budget
     // of at least 48 KB that holds one cell of every template
     int threads = 256;
     if (const char* e = std::getenv("TSR_CELL_THREADS")) {
         int v = std::atoi(e);
-        if (v >= 64 && v <= 256 && v % 32 == 0) threads = v;
+        if (v >= 64 && v <= 1024 && v % 32 == 0) threads = v;
     }
     return tsr::plan_cells(c, threads, 48 * 1024);
 }
@@ -534,6 +546,13 @@ int alloc_work(tsr_ctx* c, int max_krylov)
     CK(cudaMallocHost(&c->h_scal, sizeof(double) * nscal));
     CK(cudaMallocHost(&c->h_coef, sizeof(double) * 2 * (kMaxKrylovCap + 2)));
     CK(cudaMallocHost(&c->h_flag, sizeof(int) * 4));
+    CK(cudaMallocHost(&c->h_eps, sizeof(double) * 2));
+    c->u_base = c->d_u;
+    for (int par = 0; par < 2; ++par) {
+        c->graphs[par].assign((size_t)(maxk > 0 ? maxk : 1), nullptr);
+        c->graph_ev[par].resize((size_t)(maxk > 0 ? maxk : 1));
+        for (auto& a : c->graph_ev[par]) a.fill(nullptr);
+    }
     c->Hm.assign((size_t)c->ldH * (size_t)(maxk > 0 ? maxk : 1), 0.0);
     c->phi.assign((size_t)(maxk > 0 ? maxk : 1) * (size_t)(maxk > 0 ? maxk : 1), 0.0);
     return TSR_OK;
@@ -565,6 +584,17 @@ int fetch_scalar(tsr_ctx* c, int slot, double* out)
 double* scal_slot(tsr_ctx* c, int slot)
 {
     return c->d_scal + (size_t)c->ldH * (size_t)(c->maxk > 0 ? c->maxk : 1) + slot;
+}
+
+// device copy of {eps, 1/eps} for the finite-difference kernels
+int set_eps(tsr_ctx* c, double eps)
+{
+    CK(cudaStreamSynchronize(c->stream));   // the staging buffer may still be in flight
+    c->h_eps[0] = eps;
+    c->h_eps[1] = 1.0 / eps;
+    CK(cudaMemcpyAsync(scal_slot(c, S_EPS), c->h_eps, 2 * sizeof(double), cudaMemcpyHostToDevice,
+                       c->stream));
+    return TSR_OK;
 }
 
 constexpr size_t kProfMax = 16384;
@@ -653,6 +683,14 @@ extern "C" void tsr_free(tsr_ctx* c)
     }
     for (auto& e : c->marks)
         if (e) cudaEventDestroy(e);
+    for (int par = 0; par < 2; ++par) {
+        for (auto& g : c->graphs[par])
+            if (g) cudaGraphExecDestroy(g);
+        for (auto& a : c->graph_ev[par])
+            for (auto& e : a)
+                if (e) cudaEventDestroy(e);
+    }
+    if (c->h_eps) cudaFreeHost(c->h_eps);
     for (void* p : c->allocs) cudaFree(p);
     if (c->h_scal) cudaFreeHost(c->h_scal);
     if (c->h_coef) cudaFreeHost(c->h_coef);
@@ -667,7 +705,7 @@ extern "C" int tsr_num_unknowns(tsr_ctx* c) { return c ? (int)c->N : 0; }
 extern "C" int tsr_g_eval_device(tsr_ctx* c, const double* d_u, double* d_g)
 {
     if (!c || !d_u || !d_g) return TSR_ERR_ARG;
-    launch_g(c->P, 0, d_u, nullptr, nullptr, 0.0, 0.0, d_g, c->stream);
+    launch_g(c->P, 0, d_u, nullptr, nullptr, nullptr, d_g, c->stream);
     CK(cudaGetLastError());
     return TSR_OK;
 }
@@ -676,7 +714,9 @@ extern "C" int tsr_jv_device(tsr_ctx* c, const double* d_u, const double* d_g0, 
                              double eps, double* d_w)
 {
     if (!c || !d_u || !d_g0 || !d_v || !d_w || !(eps != 0.0)) return TSR_ERR_ARG;
-    launch_g(c->P, 1, d_u, d_v, d_g0, eps, 1.0 / eps, d_w, c->stream);
+    int rc = set_eps(c, eps);
+    if (rc) return rc;
+    launch_g(c->P, 1, d_u, d_v, d_g0, scal_slot(c, S_EPS), d_w, c->stream);
     CK(cudaGetLastError());
     return TSR_OK;
 }
@@ -688,7 +728,7 @@ extern "C" int tsr_g_eval(tsr_ctx* c, const double* u, double* g)
     int rc;
     if ((rc = reset_flag(c))) return rc;
     CK(cudaMemcpyAsync(c->d_x, u, bytes, cudaMemcpyHostToDevice, c->stream));
-    launch_g(c->P, 0, c->d_x, nullptr, nullptr, 0.0, 0.0, c->d_y, c->stream);
+    launch_g(c->P, 0, c->d_x, nullptr, nullptr, nullptr, c->d_y, c->stream);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(g, c->d_y, bytes, cudaMemcpyDeviceToHost, c->stream));
     int flag = 0;
@@ -708,7 +748,9 @@ extern "C" int tsr_jv(tsr_ctx* c, const double* u, const double* g0, const doubl
     CK(cudaMemcpyAsync(c->d_x, u, bytes, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(c->d_w, v, bytes, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(c->d_g1, g0, bytes, cudaMemcpyHostToDevice, c->stream));
-    launch_g(c->P, 1, c->d_x, c->d_w, c->d_g1, eps, 1.0 / eps, c->d_y, c->stream);
+    int rc = set_eps(c, eps);
+    if (rc) return rc;
+    launch_g(c->P, 1, c->d_x, c->d_w, c->d_g1, scal_slot(c, S_EPS), c->d_y, c->stream);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(w, c->d_y, bytes, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -780,6 +822,44 @@ int phi_host(tsr_ctx* c, double alpha, int m)
 
 }  // namespace
 
+namespace {
+
+// The kernels of Arnoldi step j: w = J v_j (finite differences), modified
+// Gram-Schmidt against v_0..v_j, h_{j+1,j} = ||w||, v_{j+1} = w / h_{j+1,j}
+// and the weighted norm of v_{j+1}.  ev (4 events or null) brackets the Jv
+// and the Gram-Schmidt block; otherwise the profiling pool does.
+void arnoldi_kernels(tsr_ctx* c, int j, cudaEvent_t* ev)
+{
+    const long long N = c->N;
+    cudaStream_t s = c->stream;
+    double* V = c->d_V;
+    double* Hc = c->d_scal + (size_t)j * c->ldH;
+    int pe = -1;
+    // inside a capture, only "external" records become event-record nodes
+    if (ev) cudaEventRecordWithFlags(ev[0], s, cudaEventRecordExternal);
+    else pe = prof_begin(c, 0, g_bytes(c, true));
+    launch_g(c->P, 1, c->d_u, V + (size_t)j * N, c->d_g0, scal_slot(c, S_EPS), c->d_w, s);
+    if (ev) {
+        cudaEventRecordWithFlags(ev[1], s, cudaEventRecordExternal);
+        cudaEventRecordWithFlags(ev[2], s, cudaEventRecordExternal);
+    } else {
+        prof_end(c, pe);
+        pe = prof_begin(c, 1, 8.0 * (double)N * (double)(j + 3));   // algorithmic minimum
+    }
+    launch_dot(c->d_w, V, N, Hc, c->rw, s);
+    for (int i = 0; i <= j; ++i) {
+        const double* vnext = (i < j) ? V + (size_t)(i + 1) * N : nullptr;
+        double* res = (i < j) ? Hc + i + 1 : scal_slot(c, S_HSQ);
+        launch_mgs(c->d_w, V + (size_t)i * N, Hc + i, vnext, N, res, c->rw, s);
+    }
+    launch_scale_wsq(c->d_w, scal_slot(c, S_HSQ), Hc + j + 1, scal_slot(c, S_IH),
+                     V + (size_t)(j + 1) * N, c->d_winv, N, scal_slot(c, S_SV), c->rw, s);
+    if (ev) cudaEventRecordWithFlags(ev[3], s, cudaEventRecordExternal);
+    else prof_end(c, pe);
+}
+
+}  // namespace
+
 extern "C" int tsr_exprem_advance(tsr_ctx* c, double tend, const double* tspan, double* tspan_solns,
                                   const exprem_options_struct* opt, exprem_stats_struct* st,
                                   double* t_out)
@@ -821,7 +901,7 @@ extern "C" int tsr_exprem_advance(tsr_ctx* c, double tend, const double* tspan, 
     if (!c->g0_valid) {
         if ((rc = reset_flag(c))) return rc;
         int pe = prof_begin(c, 0, g_bytes(c, false));
-        launch_g(c->P, 0, c->d_u, nullptr, nullptr, 0.0, 0.0, c->d_g0, s);
+        launch_g(c->P, 0, c->d_u, nullptr, nullptr, nullptr, c->d_g0, s);
         prof_end(c, pe);
         CK(cudaGetLastError());
         st->FuncEvals++;
@@ -850,30 +930,50 @@ extern "C" int tsr_exprem_advance(tsr_ctx* c, double tend, const double* tspan, 
     if (beta != 0.0) {
         const double ib = 1.0 / beta;
         launch_scale(c->d_g0, ib, V, N, s);
+        if ((rc = set_eps(c, eps))) return rc;
+        const int par = (c->d_u == c->u_base) ? 0 : 1;
         for (int j = 0; j < maxk; ++j) {
-            const double* vj = V + (size_t)j * N;
-            int pe = prof_begin(c, 0, g_bytes(c, true));
-            launch_g(c->P, 1, c->d_u, vj, c->d_g0, eps, 1.0 / eps, c->d_w, s);
-            prof_end(c, pe);
-            st->FuncEvals++;
             double* Hc = Hd + (size_t)j * ldH;
-            // Gram-Schmidt block; algorithmic minimum 8 N (j + 3) bytes
-            pe = prof_begin(c, 1, 8.0 * (double)N * (double)(j + 3));
-            launch_dot(c->d_w, V, N, Hc, c->rw, s);
-            for (int i = 0; i <= j; ++i) {
-                const double* vnext = (i < j) ? V + (size_t)(i + 1) * N : nullptr;
-                double* res = (i < j) ? Hc + i + 1 : scal_slot(c, S_HSQ);
-                launch_mgs(c->d_w, V + (size_t)i * N, Hc + i, vnext, N, res, c->rw, s);
-            }
             double* vn = V + (size_t)(j + 1) * N;
-            launch_scale_wsq(c->d_w, scal_slot(c, S_HSQ), Hc + j + 1, scal_slot(c, S_IH), vn,
-                             c->d_winv, N, scal_slot(c, S_SV), c->rw, s);
-            prof_end(c, pe);
+            if (c->use_graphs) {
+                cudaGraphExec_t& ge = c->graphs[par][(size_t)j];
+                std::array<cudaEvent_t, 4>& ev = c->graph_ev[par][(size_t)j];
+                if (!ge) {
+                    for (auto& e : ev)
+                        if (!e) CK(cudaEventCreate(&e));
+                    set_counting(false);
+                    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+                    arnoldi_kernels(c, j, ev.data());
+                    cudaGraph_t g = nullptr;
+                    cudaError_t ce = cudaStreamEndCapture(s, &g);
+                    set_counting(true);
+                    CK(ce);
+                    CK(cudaGraphInstantiate(&ge, g, 0));
+                    CK(cudaGraphDestroy(g));
+                }
+                CK(cudaGraphLaunch(ge, s));
+                add_launches(j + 6);
+            } else {
+                arnoldi_kernels(c, j, nullptr);
+            }
+            st->FuncEvals++;
             CK(cudaGetLastError());
             // column j of H and the weighted norm of v_{j+1}
             CK(cudaMemcpyAsync(c->h_scal, Hc, sizeof(double) * (size_t)(j + 2), cudaMemcpyDeviceToHost, s));
             CK(cudaMemcpyAsync(c->h_scal + ldH, scal_slot(c, S_SV), sizeof(double), cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
+            if (c->use_graphs && c->prof) {
+                std::array<cudaEvent_t, 4>& ev = c->graph_ev[par][(size_t)j];
+                float a = 0.f, b = 0.f;
+                CK(cudaEventElapsedTime(&a, ev[0], ev[1]));
+                CK(cudaEventElapsedTime(&b, ev[2], ev[3]));
+                c->prof_acc_ms[0] += a;
+                c->prof_acc_bytes[0] += g_bytes(c, true);
+                c->prof_acc_n[0] += 1;
+                c->prof_acc_ms[1] += b;
+                c->prof_acc_bytes[1] += 8.0 * (double)N * (double)(j + 3);
+                c->prof_acc_n[1] += 1;
+            }
             double hs = 0.0;
             for (int i = 0; i <= j; ++i) {
                 const double hij = c->h_scal[i];
@@ -921,7 +1021,7 @@ extern "C" int tsr_exprem_advance(tsr_ctx* c, double tend, const double* tspan, 
         }
         if ((rc = reset_flag(c))) return rc;
         int pe = prof_begin(c, 0, g_bytes(c, false));
-        launch_g(c->P, 0, c->d_unew, nullptr, nullptr, 0.0, 0.0, c->d_g1, s);
+        launch_g(c->P, 0, c->d_unew, nullptr, nullptr, nullptr, c->d_g1, s);
         prof_end(c, pe);
         st->FuncEvals++;
         double err = 0.0;
@@ -1094,6 +1194,11 @@ extern "C" int tsr_profile(tsr_ctx* c, int enable)
     CK(cudaStreamSynchronize(c->stream));
     c->prof = enable != 0;
     c->prof_used = 0;
+    for (int q = 0; q < 2; ++q) {
+        c->prof_acc_ms[q] = 0.0;
+        c->prof_acc_bytes[q] = 0.0;
+        c->prof_acc_n[q] = 0;
+    }
     return TSR_OK;
 }
 
@@ -1111,6 +1216,11 @@ extern "C" int tsr_profile_read(tsr_ctx* c, int cat, double* ms, long long* coun
         t += x;
         b += e.bytes;
         ++n;
+    }
+    if (cat == 0 || cat == 1) {
+        t += c->prof_acc_ms[cat];
+        b += c->prof_acc_bytes[cat];
+        n += c->prof_acc_n[cat];
     }
     *ms = t;
     *count = n;
@@ -1183,7 +1293,7 @@ extern "C" int tsr_autotune(tsr_ctx* c, const double* u_host, int reps, double* 
     if (!c || !u_host) return TSR_ERR_ARG;
     if (reps < 1) reps = 3;
     CK(cudaMemcpyAsync(c->d_x, u_host, sizeof(double) * (size_t)c->N, cudaMemcpyHostToDevice, c->stream));
-    const int thr[] = {128, 256};
+    const int thr[] = {128, 256, 512, 1024};
     const int bud[] = {48 * 1024, 64 * 1024, 96 * 1024, 144 * 1024, 200 * 1024};
     double best = 1e30;
     int bt = c->tuned_threads, bb = c->tuned_budget;
@@ -1194,10 +1304,10 @@ extern "C" int tsr_autotune(tsr_ctx* c, const double* u_host, int reps, double* 
         for (int B : bud) {
             if (B > c->dev_smem) continue;
             if (tsr::plan_cells(c, T, B) != TSR_OK) continue;
-            launch_g(c->P, 0, c->d_x, nullptr, nullptr, 0.0, 0.0, c->d_y, c->stream);   // warm
+            launch_g(c->P, 0, c->d_x, nullptr, nullptr, nullptr, c->d_y, c->stream);   // warm
             CK(cudaEventRecord(e0, c->stream));
             for (int r = 0; r < reps; ++r)
-                launch_g(c->P, 0, c->d_x, nullptr, nullptr, 0.0, 0.0, c->d_y, c->stream);
+                launch_g(c->P, 0, c->d_x, nullptr, nullptr, nullptr, c->d_y, c->stream);
             CK(cudaEventRecord(e1, c->stream));
             CK(cudaEventSynchronize(e1));
             CK(cudaGetLastError());
@@ -1216,5 +1326,12 @@ extern "C" int tsr_autotune(tsr_ctx* c, const double* u_host, int reps, double* 
     if (best_ms) *best_ms = best;
     if (best_threads) *best_threads = bt;
     if (best_budget) *best_budget = bb;
+    return TSR_OK;
+}
+
+extern "C" int tsr_set_graphs(tsr_ctx* c, int enable)
+{
+    if (!c) return TSR_ERR_ARG;
+    c->use_graphs = enable != 0;
     return TSR_OK;
 }

@@ -96,9 +96,10 @@ int configure_cell_kernels(const Problem& P, int* occ);
 
 // Two-scale G (mode 0) or finite-difference Jv (mode 1):
 //   mode 0: out = G(u)
-//   mode 1: out = (G(u + eps v) - g0) * inv_eps
+//   mode 1: out = (G(u + eps v) - g0) * inv_eps, with epsv = {eps, inv_eps}
+//           in device memory
 void launch_g(const Problem& P, int mode, const double* u, const double* v, const double* g0,
-              double eps, double inv_eps, double* out, cudaStream_t s);
+              const double* epsv, double* out, cudaStream_t s);
 
 // Fixed-order reductions (result written to device scalar *res).
 struct RedWork {
@@ -126,6 +127,8 @@ void launch_err(const double* g1, const double* g0, const double* V, long long l
                 cudaStream_t s);
 // number of kernels this library has launched (host counter)
 unsigned long long kernel_launches();
+void add_launches(int n);
+void set_counting(bool on);
 // measured FP64 instruction rate of the device (DFMA chains)
 int measure_fp64_peak(double* ops_per_s);
 

@@ -31,10 +31,18 @@ namespace tsr {
 
 __device__ const tsr_math_tables d_tables = TSR_MATH_TABLES_INIT;
 
-// host-side count of every kernel this library launches
+// host-side count of every kernel this library launches (a graph replay
+// adds the kernels it contains; kernels recorded during capture are not
+// launches)
 static unsigned long long g_launches = 0;
+static bool g_counting = true;
 unsigned long long kernel_launches() { return g_launches; }
-static inline void count(int n = 1) { g_launches += (unsigned long long)n; }
+void add_launches(int n) { g_launches += (unsigned long long)n; }
+void set_counting(bool on) { g_counting = on; }
+static inline void count(int n = 1)
+{
+    if (g_counting) g_launches += (unsigned long long)n;
+}
 
 static constexpr int kTabDoubles = (int)(sizeof(tsr_math_tables) / sizeof(double));
 
@@ -235,11 +243,16 @@ __device__ __forceinline__ void macro_element_terms(const Problem& P, int k, con
 // spaces.  Every cell still follows the single-cell operation sequence (the
 // same as the host oracle), so packing changes speed, never bits.
 template <int MODE>
-__global__ void __launch_bounds__(256) k_cells(Problem P, const double* __restrict__ u,
-                                               const double* __restrict__ v,
-                                               const double* __restrict__ g0, double eps,
-                                               double inv_eps, double* __restrict__ out)
+__global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restrict__ u,
+                                                const double* __restrict__ v,
+                                                const double* __restrict__ g0,
+                                                const double* __restrict__ epsv,
+                                                double* __restrict__ out)
 {
+    // finite-difference step and its reciprocal, from device memory so that
+    // a captured graph replays with the current values
+    const double eps = MODE ? epsv[0] : 0.0;
+    const double inv_eps = MODE ? epsv[1] : 0.0;
     extern __shared__ double sm[];
     tsr_math_tables* T = reinterpret_cast<tsr_math_tables*>(sm);
     double* misc = sm + kTabDoubles;                         // 16 per cell slot
@@ -405,9 +418,12 @@ __global__ void __launch_bounds__(256) k_cells(Problem P, const double* __restri
 template <int MODE>
 __global__ void __launch_bounds__(128) k_macro_nodes(Problem P, const double* __restrict__ u,
                                                      const double* __restrict__ v,
-                                                     const double* __restrict__ g0, double eps,
-                                                     double inv_eps, double* __restrict__ out)
+                                                     const double* __restrict__ g0,
+                                                     const double* __restrict__ epsv,
+                                                     double* __restrict__ out)
 {
+    const double eps = MODE ? epsv[0] : 0.0;
+    const double inv_eps = MODE ? epsv[1] : 0.0;
     __shared__ tsr_math_tables T;
     load_tables(&T);
     __syncthreads();
@@ -457,16 +473,16 @@ int configure_cell_kernels(const Problem& P, int* occ)
 }
 
 void launch_g(const Problem& P, int mode, const double* u, const double* v, const double* g0,
-              double eps, double inv_eps, double* out, cudaStream_t s)
+              const double* epsv, double* out, cudaStream_t s)
 {
     const int nb = (P.M.Mn + 127) / 128;
     count(2);
     if (mode == 0) {
-        k_cells<0><<<P.micro_grid, P.micro_block, P.micro_smem, s>>>(P, u, v, g0, eps, inv_eps, out);
-        k_macro_nodes<0><<<nb, 128, 0, s>>>(P, u, v, g0, eps, inv_eps, out);
+        k_cells<0><<<P.micro_grid, P.micro_block, P.micro_smem, s>>>(P, u, v, g0, epsv, out);
+        k_macro_nodes<0><<<nb, 128, 0, s>>>(P, u, v, g0, epsv, out);
     } else {
-        k_cells<1><<<P.micro_grid, P.micro_block, P.micro_smem, s>>>(P, u, v, g0, eps, inv_eps, out);
-        k_macro_nodes<1><<<nb, 128, 0, s>>>(P, u, v, g0, eps, inv_eps, out);
+        k_cells<1><<<P.micro_grid, P.micro_block, P.micro_smem, s>>>(P, u, v, g0, epsv, out);
+        k_macro_nodes<1><<<nb, 128, 0, s>>>(P, u, v, g0, epsv, out);
     }
 }
 
