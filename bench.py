@@ -150,7 +150,9 @@ def allsum(dist, x):
 
 def make_problem(args):
     from twoscalerich_gb300 import problem as P
-    if args.config == 3:
+    if args.config == 4:
+        p = P.config4(scenarios=args.scenarios, n_macro=args.n_macro, n_micro=args.n_micro)
+    elif args.config == 3:
         p = P.config3(n_macro=args.n_macro)
     else:
         p = P.config2(n_macro=args.n_macro, n_micro=args.n_micro)
@@ -168,6 +170,17 @@ def l2_statement(args, N):
 
 
 def workload(args, N):
+    if args.config == 4:
+        return {"workload": "two-scale Richards ensemble, independent EXPREM per scenario",
+                "scenarios": args.scenarios,
+                "macro_nodes": "%dx%d per scenario" % (args.n_macro, args.n_macro),
+                "micro_nodes_per_cell": "%dx%d" % (args.n_micro, args.n_micro),
+                "cells": args.scenarios * 2 * (args.n_macro - 1) ** 2, "unknowns": N,
+                "max_krylov": args.max_krylov, "tol": 1e-6, "t_end_days": 1.0,
+                "per_scenario": "Ks_A ~ LogNormal(ln 0.054, 0.5), Ks_B ~ LogNormal(ln 0.001, 0.5), "
+                                "alpha_A ~ U(1.5, 4), n_A ~ U(1.8, 2.6), h0 ~ U(-10, -1) m",
+                "inputs_vs_l2": l2_statement(args, N),
+                "parallelism": "replicas" if WORLD > 1 else "1 GPU", "packing": "autotuned"}
     if args.config == 3:
         return {"workload": "two-scale Richards, batched uneven micro meshes, EXPREM steps",
                 "macro_nodes": "%dx%d" % (args.n_macro, args.n_macro),
@@ -376,6 +389,150 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def cpu_ensemble_rate(ens, seconds, threads=None):
+    """Scenario-steps per second of the oracle's OpenMP EXPREM (C-library
+    log/exp) on scenario 0 alone, stepped from t = 0 for about `seconds`."""
+    import oracle
+    from twoscalerich_gb300 import capi
+    from twoscalerich_gb300 import problem as P
+    threads = threads or os.cpu_count() or 1
+    p = P.scenario_problem(ens, 0)
+    o = oracle.Oracle(p, nthreads=threads, libm=True)
+    u = p.u0.copy()
+    st = capi.ExpremStats()
+    solns = np.zeros(p.N)
+    t, steps = 0.0, 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds and t < p.tend:
+        t = o.exprem_step(t, u, p.tspan, solns, p.options, st)
+        steps += 1
+    el = time.perf_counter() - t0
+    o.close()
+    return {"value": steps / el, "unit": "scenario-steps/s", "cores": threads, "kind": "port",
+            "sample": "%d accepted EXPREM steps of scenario 0 (%d unknowns) from t = 0 by the "
+                      "oracle's OpenMP form with C-library log/exp (%.1f s)" % (steps, p.N, el)}
+
+
+def run_ensemble(args):
+    """Config 4: all scenarios advance in lockstep rounds (each scenario one
+    accepted step of its own size per round).  value = scenario-steps per
+    second over the timed rounds; with --to-end the run continues until every
+    scenario reaches t_end and reports the p50/p95 per-scenario wall time."""
+    from twoscalerich_gb300 import capi
+    from twoscalerich_gb300 import problem as P
+    dist = dist_init()
+    lib = capi.load()
+    p = make_problem(args)
+    N, S = p.N, p.S
+    ctx = P.Context(p, max_krylov=p.options.MaxKrylov)
+    h = ctx.h
+    tuned = ctx.autotune(p.u0, reps=2)
+    stats = (capi.ExpremStats * S)()
+    ctx.load(p.u0)
+    for _ in range(args.warmup):
+        ctx.ensemble_advance(stats)
+    steps0 = sum(stats[s].NumSteps for s in range(S))
+    evals0 = sum(stats[s].FuncEvals for s in range(S))
+    clocks = Clocks()
+    clocks.start()
+    barrier(dist)
+    capi.check(lib.tsr_sync(h), "sync")
+    capi.check(lib.tsr_profile(h, 1), "profile")
+    launches0 = lib.tsr_kernel_launches()
+    capi.check(lib.tsr_mark(h, 0), "mark")
+    t0 = time.perf_counter()
+    round_s = []
+    for _ in range(args.steps):
+        r0 = time.perf_counter()
+        t, status, nrun = ctx.ensemble_advance(stats)
+        round_s.append(time.perf_counter() - r0)
+    capi.check(lib.tsr_mark(h, 1), "mark")
+    capi.check(lib.tsr_sync(h), "sync")
+    launches = lib.tsr_kernel_launches() - launches0
+    barrier(dist)
+    clk = clocks.stop()
+    ms = C.c_double()
+    capi.check(lib.tsr_elapsed_ms(h, 0, 1, C.byref(ms)), "elapsed")
+    steps = sum(stats[s].NumSteps for s in range(S)) - steps0
+    evals = sum(stats[s].FuncEvals for s in range(S)) - evals0
+    t_max = allmax(dist, ms.value / 1e3)
+    value = allsum(dist, steps) / t_max
+    gms, gcount, gbytes = C.c_double(), C.c_longlong(), C.c_double()
+    capi.check(lib.tsr_profile_read(h, 0, C.byref(gms), C.byref(gcount), C.byref(gbytes)), "prof")
+    capi.check(lib.tsr_profile(h, 0), "profile")
+    hbm_peak, peak_src = measured_peaks()
+    g_avg_ms = gms.value / max(gcount.value, 1)
+    g_gbs = gbytes.value / max(gms.value * 1e-3, 1e-30) / 1e9
+    # e2e: state from pinned host memory in and out around every round
+    u_host = capi.PinnedArray(N)
+    capi.check(lib.tsr_exprem_store(h, u_host.a.ctypes.data_as(capi.dp)), "store")
+    tq = np.array([stats[s].CurrentTime for s in range(S)])
+    e_steps0 = sum(stats[s].NumSteps for s in range(S))
+    capi.check(lib.tsr_sync(h), "sync")
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
+        capi.check(lib.tsr_ensemble_load(h, u_host.a.ctypes.data_as(capi.dp), capi.ptr(tq)), "load")
+        tq, _, _ = ctx.ensemble_advance(stats)
+        capi.check(lib.tsr_exprem_store(h, u_host.a.ctypes.data_as(capi.dp)), "store")
+    e_wall = time.perf_counter() - w0
+    e2e_value = (sum(stats[s].NumSteps for s in range(S)) - e_steps0) / e_wall
+    u_host.free()
+    to_end = None
+    if args.to_end:
+        # restart from t = 0 and run every scenario to t_end
+        ctx.load(p.u0)
+        st2 = (capi.ExpremStats * S)()
+        done_at = [None] * S
+        w0 = time.perf_counter()
+        rounds = 0
+        while True:
+            t, status, nrun = ctx.ensemble_advance(st2)
+            rounds += 1
+            now = time.perf_counter() - w0
+            for s in range(S):
+                if done_at[s] is None and (t[s] >= p.tend or status[s] != 0):
+                    done_at[s] = now
+            if nrun == 0:
+                break
+        wall = sorted(done_at)
+        to_end = {"rounds": rounds, "wall_s_total": wall[-1],
+                  "p50_scenario_wall_s": float(np.percentile(wall, 50)),
+                  "p95_scenario_wall_s": float(np.percentile(wall, 95)),
+                  "steps_per_scenario": [st2[s].NumSteps for s in range(S)],
+                  "failed": int(sum(1 for s in range(S) if status[s] != 0)),
+                  "scenario_steps_per_s": sum(st2[s].NumSteps for s in range(S)) / wall[-1]}
+    cpu = None
+    if RANK == 0 and WORLD == 1 and not args.no_cpu_baseline:
+        cpu = cpu_ensemble_rate(p, args.cpu_seconds)
+    line = {
+        "metric": "scenario-steps/s (accepted EXPREM steps summed over scenarios per second)",
+        "value": value, "unit": "scenario-steps/s", "n_gpus": WORLD, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_max / max(args.steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded generator 20261203, evaluation seed 7)",
+        "config": workload(args, N),
+        "g_evals_per_s": allsum(dist, evals) / t_max,
+        "round_wall_s": {"p50": float(np.percentile(round_s, 50)), "p95": float(np.percentile(round_s, 95))},
+        "to_end": to_end,
+        "roofline": {"bound": "hbm", "kernel": "G / Jv evaluation (k_cells + k_macro_nodes)",
+                     "achieved": g_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": g_gbs / hbm_peak,
+                     "peak_source": peak_src, "traffic": None, "avg_launch_ms": g_avg_ms,
+                     "launches": gcount.value},
+        "clocks": clk,
+        "e2e": {"value": e2e_value, "unit": "scenario-steps/s", "h2d_bytes_per_step": 8 * N,
+                "d2h_bytes_per_step": 8 * N,
+                "note": "state reloaded from host each round, so every round re-evaluates G(u)"},
+        "gpu_launches": int(launches),
+        "autotuned": {"g_ms": tuned[0], "threads": tuned[1], "smem_budget": tuned[2]},
+        "cpu_baseline": cpu,
+    }
+    if RANK == 0:
+        print(json.dumps(line))
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 # FP64 instructions (DADD + DMUL + DFMA, thread level) per unknown of one
 # finite-difference Jv launch of the cell kernel, and its DRAM bytes (read +
 # write) per unknown, from the ncu capture of the 141x141 / 21x21 case in
@@ -396,15 +553,27 @@ def main():
     ap.add_argument("--cpu-evals", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--max-krylov", type=int, default=None)
-    ap.add_argument("--config", type=int, default=2, choices=[2, 3],
-                    help="2: 201x201 x 21x21 plain method; 3: 151x151 batched uneven cells")
+    ap.add_argument("--config", type=int, default=2, choices=[2, 3, 4],
+                    help="2: 201x201 x 21x21 plain method; 3: 151x151 batched uneven cells; "
+                         "4: 64-scenario ensemble of 51x51 x 15x15")
+    ap.add_argument("--scenarios", type=int, default=64)
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--to-end", action="store_true",
+                    help="config 4: also run every scenario to t_end (p50/p95 wall time)")
     args = ap.parse_args()
     if args.config == 3 and args.n_macro == 201:
         args.n_macro = 151
+    if args.config == 4:
+        if args.n_macro == 201:
+            args.n_macro = 51
+        if args.n_micro == 21:
+            args.n_micro = 15
     if args.max_krylov is None:
-        args.max_krylov = 30 if args.config == 3 else 40
+        args.max_krylov = 30 if args.config in (3, 4) else 40
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == 4:
+        run_ensemble(args)
     else:
         run_ours(args)
 

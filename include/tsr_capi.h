@@ -155,6 +155,33 @@ int tsr_exprem_advance(tsr_ctx* ctx, double tend, const double* tspan,
                        exprem_stats_struct* stats, double* t_out);
 int tsr_exprem_store(tsr_ctx* ctx, double* u_host);
 
+/* ---- ensembles (no counterpart in the reference) ------------------------
+ * A context built with tsr_model_ext.scenarios = S > 1 holds S independent
+ * problems whose unknowns are laid out scenario by scenario.  G, Jv and
+ * water entry points above act on all of them at once.  The ensemble EXPREM
+ * advances every scenario that has not reached tend by one accepted step of
+ * its own size and Krylov dimension, all in the same launches; scenario s's
+ * trajectory is the one it would have on its own (same reductions, same
+ * order).  The state is loaded and stored with tsr_exprem_load/store (all
+ * scenarios at time t). */
+int tsr_num_scenarios(tsr_ctx* ctx);
+/* unknowns [*first, *first + *count) of scenario s */
+int tsr_scenario_range(tsr_ctx* ctx, int s, long long* first, long long* count);
+/* stats, t and status are arrays of S; tspan_solns is NULL or S pointers
+ * (NULL or rows of the scenario's unknowns, row k for tspan[k]).  status[s]
+ * is TSR_OK or the error that stopped scenario s (it then stays where it
+ * stopped); *n_running counts scenarios still short of tend. */
+int tsr_ensemble_advance(tsr_ctx* ctx, double tend, const double* tspan,
+                         double* const* tspan_solns,
+                         const exprem_options_struct* options,
+                         exprem_stats_struct* stats, double* t, int* status,
+                         int* n_running);
+/* Loads the state (host, N doubles) with scenario s at time t[s]; the
+ * scenarios' statuses are kept (a stopped scenario stays stopped). */
+int tsr_ensemble_load(tsr_ctx* ctx, const double* u_host, const double* t);
+/* water content of each scenario (S doubles) */
+int tsr_ensemble_water(tsr_ctx* ctx, const double* u, double* water);
+
 /* C entry with the data of the C++ drop-in Gfunc_gpu (tsr_dropin.hpp):
  * g = G(u) for the context registered for user_data (created on first use,
  * keyed by the address of its macro element array). */

@@ -148,6 +148,15 @@ typedef struct tsr_model_ext {
     const micro_mesh_struct* templates;   /* [n_templates] */
     const int* cell_template;             /* [no_elements] */
     const soil_struct* cell_soilB;        /* [no_elements] material B per cell, NULL = soilB */
+    /* Ensemble form (no counterpart in the reference): with scenarios = S > 1
+     * the macro mesh is S identical disjoint blocks (no_nodes/S nodes and
+     * no_elements/S elements each, block s numbered after block s-1); the
+     * unknowns are laid out scenario by scenario, [macro_s | cells_s], and
+     * scenario s may carry its own material A, Keff scale and material B. */
+    int scenarios;                        /* 0 or 1: one problem */
+    int reserved2;
+    const soil_struct* scen_soilA;        /* [S] or NULL = soilA */
+    const double* scen_keff_scale;        /* [S] factor on Keff, or NULL = 1 */
 } tsr_model_ext;
 
 #endif /* TSR_TYPES_H */

@@ -43,6 +43,7 @@ def load(libm=False):
         _sig(lib, "oracle_g", C.c_int, [vp, dp, dp, C.c_int])
         _sig(lib, "oracle_jv", C.c_int, [vp, dp, dp, dp, C.c_double, dp, C.c_int])
         _sig(lib, "oracle_water", C.c_int, [vp, dp, dp])
+        _sig(lib, "oracle_water_scenarios", C.c_int, [vp, dp, dp])
         _sig(lib, "oracle_dot", C.c_double, [dp, dp, C.c_long])
         _sig(lib, "oracle_vsum", C.c_double, [dp, C.c_long])
         _sig(lib, "oracle_wsq", C.c_double, [dp, dp, C.c_long])
@@ -112,6 +113,11 @@ class Oracle:
         w = C.c_double()
         self.lib.oracle_water(self.h, self._p(u), C.byref(w))
         return w.value
+
+    def water_scenarios(self, u):
+        w = np.empty(self.p.S)
+        self.lib.oracle_water_scenarios(self.h, self._p(u), self._p(w))
+        return w
 
     def dot(self, x, y):
         return self.lib.oracle_dot(self._p(x), self._p(y), x.size)

@@ -285,6 +285,12 @@ typedef struct oracle_problem {
     long* cell_off;             /* [Ne] first unknown of cell k */
     vgpar* cell_pB;             /* [Ne] or NULL (all pB) */
     int max_mn, max_mNe;
+    /* ensemble form: S scenarios, scenario-major unknowns */
+    int S, scen_nodes, scen_cells;
+    long* node_off;             /* [Mn] unknown index of macro node i */
+    long* scen_start;           /* [S+1] */
+    vgpar* scen_pA;             /* [S] or NULL (all pA) */
+    double* scen_kscale;        /* [S] or NULL (all 1) */
     long N;
     int Mn, Ne, nv, mn, mNe;
     /* EXPREM workspace */
@@ -328,14 +334,35 @@ oracle_problem* oracle_create(const user_data_struct* ud, const tsr_model_ext* e
         P->tpl = &P->ud.micro_mesh;
         P->cell_tpl = NULL;
     }
-    /* unknown offsets: cell k follows cell k-1 */
+    /* unknown offsets, scenario by scenario: [macro nodes of s | cells of
+     * s, cell k following cell k-1]; one scenario is the reference layout */
+    P->S = (ext && ext->scenarios > 1) ? ext->scenarios : 1;
+    P->scen_nodes = P->Mn / P->S;
+    P->scen_cells = P->Ne / P->S;
     P->cell_off = (long*)malloc(sizeof(long) * (size_t)(P->Ne > 0 ? P->Ne : 1));
-    long off = P->Mn;
-    for (int k = 0; k < P->Ne; ++k) {
-        P->cell_off[k] = off;
-        off += P->tpl[P->cell_tpl ? P->cell_tpl[k] : 0].no_nodes;
+    P->node_off = (long*)malloc(sizeof(long) * (size_t)(P->Mn > 0 ? P->Mn : 1));
+    P->scen_start = (long*)malloc(sizeof(long) * (size_t)(P->S + 1));
+    long off = 0;
+    for (int s = 0; s < P->S; ++s) {
+        P->scen_start[s] = off;
+        for (int i = s * P->scen_nodes; i < (s + 1) * P->scen_nodes; ++i) P->node_off[i] = off++;
+        for (int k = s * P->scen_cells; k < (s + 1) * P->scen_cells; ++k) {
+            P->cell_off[k] = off;
+            off += P->tpl[P->cell_tpl ? P->cell_tpl[k] : 0].no_nodes;
+        }
     }
+    P->scen_start[P->S] = off;
     P->N = off;
+    P->scen_pA = NULL;
+    P->scen_kscale = NULL;
+    if (ext && ext->scen_soilA) {
+        P->scen_pA = (vgpar*)malloc(sizeof(vgpar) * (size_t)P->S);
+        for (int s = 0; s < P->S; ++s) P->scen_pA[s] = make_vgpar(&ext->scen_soilA[s]);
+    }
+    if (ext && ext->scen_keff_scale) {
+        P->scen_kscale = (double*)malloc(sizeof(double) * (size_t)P->S);
+        for (int s = 0; s < P->S; ++s) P->scen_kscale[s] = ext->scen_keff_scale[s];
+    }
     P->inv_Y = 1.0 / P->tpl[0].cell_area;
     P->cell_pB = NULL;
     if (ext && ext->cell_soilB) {
@@ -383,12 +410,19 @@ void oracle_destroy(oracle_problem* P)
     free(P->faceD);
     free(P->cell_off);
     free(P->cell_pB);
+    free(P->node_off);
+    free(P->scen_start);
+    free(P->scen_pA);
+    free(P->scen_kscale);
     free(P->V); free(P->Hm); free(P->phi); free(P->g0); free(P->g1); free(P->w);
     free(P->unew); free(P->winv); free(P->x); free(P->D); free(P->Dt);
     free(P);
 }
 
 long oracle_num_unknowns(const oracle_problem* P) { return P->N; }
+
+/* first unknown of scenario s (s = S gives N) */
+long oracle_scenario_start(const oracle_problem* P, int s) { return P->scen_start[s]; }
 
 int oracle_dirichlet_mask(const oracle_problem* P, unsigned char* out)
 {
@@ -404,9 +438,10 @@ static void interp_coeffs(const oracle_problem* P, const double* H, int k, doubl
     const macro_mesh_struct* M = &P->ud.macro_mesh;
     int nv = P->nv, Ne = P->Ne;
     for (int m = 0; m < nv; ++m) {
-        double a = M->shape_funcs[(size_t)(m * nv + 0) * Ne + k] * H[M->elements[k]];
+        double a = M->shape_funcs[(size_t)(m * nv + 0) * Ne + k] * H[P->node_off[M->elements[k]]];
         for (int i = 1; i < nv; ++i)
-            a = fma(M->shape_funcs[(size_t)(m * nv + i) * Ne + k], H[M->elements[(size_t)i * Ne + k]], a);
+            a = fma(M->shape_funcs[(size_t)(m * nv + i) * Ne + k],
+                    H[P->node_off[M->elements[(size_t)i * Ne + k]]], a);
         al[m] = a;
     }
 }
@@ -577,6 +612,8 @@ int oracle_g(oracle_problem* P, const double* x, double* g, int nthreads)
             double Hf = interp_at(nv, al, mx, my);
             double K[4];
             keff_eval(Hf, &P->kp, K);
+            if (P->scen_kscale)
+                for (int q = 0; q < 4; ++q) K[q] *= P->scen_kscale[k / P->scen_cells];
             double gy1 = gy + 1.0;
             double qx = fma(K[0], gx, K[1] * gy1);
             double qy = fma(K[2], gx, K[3] * gy1);
@@ -603,6 +640,8 @@ int oracle_g(oracle_problem* P, const double* x, double* g, int nthreads)
                     double Hb = interp_at(nv, al, bx, by);
                     double K[4];
                     keff_eval(Hb, &P->kp, K);
+                    if (P->scen_kscale)
+                        for (int q = 0; q < 4; ++q) K[q] *= P->scen_kscale[k / P->scen_cells];
                     double gy1 = gy + 1.0;
                     double qx = fma(K[0], gx, K[1] * gy1);
                     double qy = fma(K[2], gx, K[3] * gy1);
@@ -619,15 +658,17 @@ int oracle_g(oracle_problem* P, const double* x, double* g, int nthreads)
         }
     }
     for (int i = 0; i < Mn; ++i) {
+        const long o = P->node_off[i];
         if (P->dirichlet[i]) {
-            g[i] = 0.0;
+            g[o] = 0.0;
             continue;
         }
+        const vgpar* pA = P->scen_pA ? &P->scen_pA[i / P->scen_nodes] : &P->pA;
         double K, Cn, Cd, Se;
-        vg_eval(x[i], &P->pA, &K, &Cn, &Cd, &Se);
+        vg_eval(x[o], pA, &K, &Cn, &Cd, &Se);
         double A = P->epsA * M->CV_area[i];
         double den = fma(P->Ss, Cd, Cn) * A;
-        g[i] = (acc[i] * Cd) / den;
+        g[o] = (acc[i] * Cd) / den;
     }
     free(acc);
     free(Q);
@@ -654,16 +695,21 @@ int oracle_jv(oracle_problem* P, const double* u, const double* g0, const double
     return rc;
 }
 
-/* total water: fixed-order sum of Mn node terms then Ne cell terms */
-int oracle_water(oracle_problem* P, const double* u, double* water)
+/* Water terms laid out scenario by scenario, [macro nodes of s | cells of
+ * s] (one scenario: Mn node terms then Ne cell terms); per-scenario sums
+ * go to per[s] when per is not NULL. */
+static int water_terms(oracle_problem* P, const double* u, double* water, double* per)
 {
     const macro_mesh_struct* M = &P->ud.macro_mesh;
     const int Mn = P->Mn, Ne = P->Ne, nv = P->nv;
     double* terms = (double*)malloc(sizeof(double) * (size_t)(Mn + Ne));
     for (int i = 0; i < Mn; ++i) {
+        const vgpar* pA = P->scen_pA ? &P->scen_pA[i / P->scen_nodes] : &P->pA;
         double K, Cn, Cd, Se;
-        vg_eval(u[i], &P->pA, &K, &Cn, &Cd, &Se);
-        terms[i] = (P->epsA * M->CV_area[i]) * fma(P->pA.dth, Se, P->pA.thr);
+        vg_eval(u[P->node_off[i]], pA, &K, &Cn, &Cd, &Se);
+        const int sc = i / P->scen_nodes;
+        terms[(size_t)sc * (P->scen_nodes + P->scen_cells) + (i - sc * P->scen_nodes)] =
+            (P->epsA * M->CV_area[i]) * fma(pA->dth, Se, pA->thr);
     }
     for (int k = 0; k < Ne; ++k) {
         const double s = P->cell_scale ? P->cell_scale[k] : 1.0;
@@ -693,11 +739,30 @@ int oracle_water(oracle_problem* P, const double* u, double* water)
         }
         double area = M->SCV_area[k];
         for (int j = 1; j < nv; ++j) area += M->SCV_area[(size_t)j * Ne + k];
-        terms[Mn + k] = (area * P->inv_Y) * ((s * s) * butterfly32(p));
+        const int sc = k / P->scen_cells;
+        terms[(size_t)sc * (P->scen_nodes + P->scen_cells) + P->scen_nodes + (k - sc * P->scen_cells)] =
+            (area * P->inv_Y) * ((s * s) * butterfly32(p));
     }
     *water = oracle_vsum(terms, (long)Mn + Ne);
+    if (per)
+        for (int sc = 0; sc < P->S; ++sc)
+            per[sc] = oracle_vsum(terms + (size_t)sc * (P->scen_nodes + P->scen_cells),
+                                  (long)P->scen_nodes + P->scen_cells);
     free(terms);
     return 0;
+}
+
+/* total water content */
+int oracle_water(oracle_problem* P, const double* u, double* water)
+{
+    return water_terms(P, u, water, NULL);
+}
+
+/* water content of each scenario (S doubles) */
+int oracle_water_scenarios(oracle_problem* P, const double* u, double* per)
+{
+    double total;
+    return water_terms(P, u, &total, per);
 }
 
 /* ------------------------------------------------------------------ */

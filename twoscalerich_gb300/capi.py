@@ -84,7 +84,8 @@ class ModelExt(C.Structure):
         ("dirichlet_h", C.c_double), ("specific_storage", C.c_double),
         ("kface_mode", C.c_int), ("n_templates", C.c_int), ("cell_scale", dp),
         ("templates", C.POINTER(MicroMesh)), ("cell_template", ip),
-        ("cell_soilB", C.POINTER(Soil)),
+        ("cell_soilB", C.POINTER(Soil)), ("scenarios", C.c_int), ("reserved2", C.c_int),
+        ("scen_soilA", C.POINTER(Soil)), ("scen_keff_scale", dp),
     ]
 
 
@@ -127,6 +128,14 @@ _SIGNATURES = {
     "tsr_exprem_advance": (C.c_int, [C.c_void_p, C.c_double, dp, dp, C.POINTER(ExpremOptions),
                                      C.POINTER(ExpremStats), dp]),
     "tsr_exprem_store": (C.c_int, [C.c_void_p, dp]),
+    "tsr_num_scenarios": (C.c_int, [C.c_void_p]),
+    "tsr_scenario_range": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_longlong),
+                                     C.POINTER(C.c_longlong)]),
+    "tsr_ensemble_advance": (C.c_int, [C.c_void_p, C.c_double, dp, C.POINTER(dp),
+                                       C.POINTER(ExpremOptions), C.POINTER(ExpremStats), dp,
+                                       C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "tsr_ensemble_water": (C.c_int, [C.c_void_p, dp, dp]),
+    "tsr_ensemble_load": (C.c_int, [C.c_void_p, dp, dp]),
     "tsr_gfunc_gpu": (C.c_int, [dp, dp, C.POINTER(UserData)]),
     "tsr_set_default_ext": (C.c_int, [C.POINTER(ModelExt), C.c_int]),
     "tsr_release_all": (None, []),

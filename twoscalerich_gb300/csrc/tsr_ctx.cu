@@ -32,8 +32,22 @@ namespace {
 constexpr double kKrylovTol = 0.1;   // Krylov error accepted as a fraction of the step tolerance
 constexpr int kMaxKrylovCap = 512;
 
-// device scalar slots after the Hessenberg block
-enum { S_HSQ = 0, S_SV, S_ERR, S_DOT, S_BETA2, S_NU2, S_WATER, S_IH, S_EPS, S_IEPS, S_COUNT = 16 };
+// device scalar slots after each scenario's Hessenberg block
+enum { S_HSQ = 0, S_SV, S_ERR, S_DOT, S_BETA2, S_NU2, S_WATER, S_IH, S_EPS, S_IEPS, S_IB, S_COUNT = 16 };
+
+// host state of one scenario's EXPREM integration (the whole problem when
+// there is one scenario)
+struct ScenState {
+    double t = 0.0;
+    bool loaded = false;
+    bool g0_valid = false;
+    int status = 0;              // TSR_OK, or the error that stopped this scenario
+    // the step in progress
+    double dt = 0.0, beta = 0.0, nu = 0.0, eps = 0.0, errK = 0.0, vnw = 0.0, err = 0.0;
+    bool last = false, happy = false, iterating = false;
+    int m = 0, maxk = 0;
+    std::vector<double> Hm, phi, cv, z;
+};
 
 }  // namespace
 
@@ -55,13 +69,24 @@ struct tsr_ctx {
     RedWork rw{};
     int maxk = 0;
     int ldH = 0;
+    // scenarios (one for the plain problem): unknowns [start_s, start_s+1)
+    int S = 1;
+    std::vector<long long> scen_start;
+    SegInfo seg{};               // the unknowns, one segment per scenario
+    SegInfo seg_terms{};         // water terms, one segment per scenario
+    int* d_active = nullptr;     // [S] scenarios the next launches work on
+    int* h_active = nullptr;     // pinned staging of d_active
+    std::vector<int> active_now; // what d_active holds
+    unsigned int* d_counters = nullptr;
+    long long HS = 0;            // doubles per scenario in d_scal (H block + slots)
+    int CS = 0;                  // doubles per scenario in d_coef: c | z | dt/3
+    int* d_mint = nullptr;       // [2S]: m_s, mz_s
+    int* h_mint = nullptr;       // pinned
+    double* h_stage = nullptr;   // pinned staging of per-scenario scalars
     // EXPREM state
-    bool state_loaded = false;
-    double t_state = 0.0;
-    bool g0_valid = false;
+    std::vector<ScenState> sc;
     const double* last_u0 = nullptr;
     double last_t = -1.0;
-    std::vector<double> Hm, phi;
     // optional event timing of the kernel classes inside EXPREM steps
     struct ProfEv {
         cudaEvent_t a, b;
@@ -80,12 +105,11 @@ struct tsr_ctx {
     int tuned_threads = 0, tuned_budget = 0;
     // finite-difference step {eps, 1/eps}, staged through pinned memory
     double* h_eps = nullptr;
-    // one captured graph per Arnoldi index j and state-buffer parity, with
-    // event nodes timing its Jv and its Gram-Schmidt block
+    // one captured graph per Arnoldi index j, with event nodes timing its
+    // Jv and its Gram-Schmidt block
     bool use_graphs = true;
-    double* u_base = nullptr;
-    std::vector<cudaGraphExec_t> graphs[2];
-    std::vector<std::array<cudaEvent_t, 4>> graph_ev[2];
+    std::vector<cudaGraphExec_t> graphs;
+    std::vector<std::array<cudaEvent_t, 4>> graph_ev;
     double prof_acc_ms[2] = {0.0, 0.0}, prof_acc_bytes[2] = {0.0, 0.0};
     long long prof_acc_n[2] = {0, 0};
 };
@@ -178,6 +202,12 @@ namespace tsr {
 int plan_cells(tsr_ctx* c, int threads, int budget)
 {
     Problem& P = c->P;
+    // captured graphs hold the old launch shape
+    for (auto& g : c->graphs)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
     const int ntpl = (int)c->tpl_host.size();
     const size_t fixed = cell_smem(kMiscSlots, 0);
     std::vector<int> per(ntpl, 1);
@@ -278,19 +308,41 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
                 return TSR_ERR_BOUNDS;
             }
     }
-    c->cell_tpl_host.assign((size_t)Ne, 0);
-    std::vector<long long> cell_off((size_t)Ne);
-    long long N = Mn;
-    for (int k = 0; k < Ne; ++k) {
-        int t = batched ? ext->cell_template[k] : 0;
-        if (t < 0 || t >= ntpl) {
-            set_error("cell_template out of range");
-            return TSR_ERR_BOUNDS;
-        }
-        c->cell_tpl_host[k] = t;
-        cell_off[k] = N;
-        N += tpls[t].no_nodes;
+    // scenarios: S disjoint blocks of the macro mesh, unknowns laid out
+    // scenario by scenario as [macro nodes of s | cells of s]
+    const int nscen = (ext && ext->scenarios > 1) ? ext->scenarios : 1;
+    if (Mn % nscen != 0 || Ne % nscen != 0) {
+        set_error("the macro mesh is not made of `scenarios` equal blocks");
+        return TSR_ERR_ARG;
     }
+    const int sn = Mn / nscen, sce = Ne / nscen;
+    if (nscen > 1)
+        for (int k = 0; k < Ne; ++k)
+            for (int j = 0; j < nv; ++j)
+                if (M.elements[(size_t)j * Ne + k] / sn != k / sce) {
+                    set_error("a macro element links two scenarios");
+                    return TSR_ERR_ARG;
+                }
+    c->S = nscen;
+    c->cell_tpl_host.assign((size_t)Ne, 0);
+    std::vector<long long> cell_off((size_t)Ne), node_off((size_t)Mn);
+    c->scen_start.assign((size_t)nscen + 1, 0);
+    long long N = 0;
+    for (int sc = 0; sc < nscen; ++sc) {
+        c->scen_start[sc] = N;
+        for (int i = sc * sn; i < (sc + 1) * sn; ++i) node_off[i] = N++;
+        for (int k = sc * sce; k < (sc + 1) * sce; ++k) {
+            int t = batched ? ext->cell_template[k] : 0;
+            if (t < 0 || t >= ntpl) {
+                set_error("cell_template out of range");
+                return TSR_ERR_BOUNDS;
+            }
+            c->cell_tpl_host[k] = t;
+            cell_off[k] = N;
+            N += tpls[t].no_nodes;
+        }
+    }
+    c->scen_start[nscen] = N;
     if (N > 0x7fffffffLL || (long long)Ne * 32 > 0x7fffffffLL) {
         set_error("problem too large for 32-bit indices");
         return TSR_ERR_ARG;
@@ -314,7 +366,25 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
     D.Ne = Ne;
     D.nv = nv;
     D.model_type = ud.model_type;
+    D.nscen = nscen;
+    D.scen_nodes = sn;
+    D.scen_cells = sce;
     int rc;
+    D.node_off = nullptr;
+    D.scen_pA = nullptr;
+    D.scen_kscale = nullptr;
+    if (nscen > 1) {
+        if ((rc = upload(c, node_off.data(), node_off.size(), &D.node_off))) return rc;
+        if (ext->scen_soilA) {
+            std::vector<VGPar> par((size_t)nscen);
+            for (int q = 0; q < nscen; ++q) par[q] = make_vg(ext->scen_soilA[q]);
+            const VGPar* dp;
+            if ((rc = upload(c, par.data(), par.size(), &dp))) return rc;
+            D.scen_pA = dp;
+        }
+        if (ext->scen_keff_scale)
+            if ((rc = upload(c, ext->scen_keff_scale, (size_t)nscen, &D.scen_kscale))) return rc;
+    }
     const size_t nvNe = (size_t)nv * Ne;
     if ((rc = upload(c, M.elements, nvNe, &D.elements))) return rc;
     if ((rc = upload(c, M.shape_funcs, (size_t)nv * nvNe, &D.sf))) return rc;
@@ -478,7 +548,7 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
         if ((rc = upload(c, cell_off.data(), cell_off.size(), &S.cell_off))) return rc;
         if ((rc = upload(c, c->cell_tpl_host.data(), c->cell_tpl_host.size(), &S.cell_tpl))) return rc;
         S.cell_par = nullptr;
-        if (batched && ext->cell_soilB) {
+        if (ext && ext->cell_soilB) {
             std::vector<VGPar> par((size_t)Ne);
             for (int k = 0; k < Ne; ++k) par[k] = make_vg(ext->cell_soilB[k]);
             const VGPar* dp;
@@ -490,9 +560,13 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
     if ((rc = dev_alloc(c, sizeof(double) * 16 * (size_t)Ne, &p))) return rc;
     P.contrib = (double*)p;
     CK(cudaMemset(P.contrib, 0, sizeof(double) * 16 * (size_t)Ne));
-    if ((rc = dev_alloc(c, sizeof(int) * 4, &p))) return rc;
+    if ((rc = dev_alloc(c, sizeof(int) * (size_t)(c->S + 3), &p))) return rc;
     P.flag = (int*)p;
-    CK(cudaMemset(P.flag, 0, sizeof(int) * 4));
+    CK(cudaMemset(P.flag, 0, sizeof(int) * (size_t)(c->S + 3)));
+    if ((rc = dev_alloc(c, sizeof(int) * (size_t)c->S, &p))) return rc;
+    c->d_active = (int*)p;
+    CK(cudaMemset(c->d_active, 0, sizeof(int) * (size_t)c->S));
+    P.active = (c->S > 1) ? c->d_active : nullptr;
     if ((rc = dev_alloc(c, sizeof(int) * 4 * (size_t)Ne, &p))) return rc;
     c->d_bundle = (int*)p;
     CK(cudaDeviceGetAttribute(&c->dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
@@ -508,9 +582,34 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
     return tsr::plan_cells(c, threads, 48 * 1024);
 }
 
+// Segments of `start` (S+1 offsets) for the reduction kernels.
+int make_seg(tsr_ctx* c, const std::vector<long long>& start, SegInfo* g)
+{
+    const int S = (int)start.size() - 1;
+    std::vector<int> block0((size_t)S + 1, 0), blkseg;
+    for (int s = 0; s < S; ++s) {
+        const int nb = reduction_blocks(start[(size_t)s + 1] - start[s]);
+        block0[(size_t)s + 1] = block0[s] + nb;
+        for (int q = 0; q < nb; ++q) blkseg.push_back(s);
+    }
+    *g = SegInfo{};
+    g->nseg = S;
+    g->nblocks = block0[S];
+    g->n1 = start[S];
+    g->counters = c->d_counters;
+    if (S == 1) return TSR_OK;    // one segment: no tables, no mask
+    int rc;
+    if ((rc = upload(c, start.data(), start.size(), &g->start))) return rc;
+    if ((rc = upload(c, block0.data(), block0.size(), &g->block0))) return rc;
+    if ((rc = upload(c, blkseg.data(), blkseg.size(), &g->blkseg))) return rc;
+    g->active = c->d_active;
+    return TSR_OK;
+}
+
 int alloc_work(tsr_ctx* c, int max_krylov)
 {
     const long long N = c->N;
+    const int S = c->S;
     void* p;
     int rc;
     double** vecs[] = {&c->d_u, &c->d_g0, &c->d_g1, &c->d_w, &c->d_unew, &c->d_winv, &c->d_x, &c->d_y};
@@ -520,81 +619,140 @@ int alloc_work(tsr_ctx* c, int max_krylov)
     }
     if ((rc = dev_alloc(c, sizeof(double) * ((size_t)c->Mn + c->Ne), &p))) return rc;
     c->d_terms = (double*)p;
+    long long nmin = N;
+    for (int s = 0; s < S; ++s) nmin = std::min(nmin, c->scen_start[(size_t)s + 1] - c->scen_start[s]);
     int maxk = max_krylov;
     if (maxk > kMaxKrylovCap) maxk = kMaxKrylovCap;
-    if (maxk > N) maxk = (int)N;
+    if (maxk > nmin) maxk = (int)nmin;
     if (maxk < 0) maxk = 0;
     c->maxk = maxk;
     c->ldH = maxk + 1;
+    const int mk1 = maxk > 0 ? maxk : 1;
     if (maxk > 0) {
         if ((rc = dev_alloc(c, sizeof(double) * (size_t)N * (size_t)(maxk + 1), &p))) return rc;
         c->d_V = (double*)p;
     }
-    const size_t nscal = (size_t)c->ldH * (size_t)(maxk > 0 ? maxk : 1) + S_COUNT;
+    c->HS = (long long)c->ldH * mk1 + S_COUNT;
+    const size_t nscal = (size_t)c->HS * (size_t)S;
     if ((rc = dev_alloc(c, sizeof(double) * nscal, &p))) return rc;
     c->d_scal = (double*)p;
     CK(cudaMemset(c->d_scal, 0, sizeof(double) * nscal));
-    if ((rc = dev_alloc(c, sizeof(double) * 2 * (kMaxKrylovCap + 2), &p))) return rc;
+    c->P.eps_stride = (int)c->HS;
+    c->CS = 2 * mk1 + 4;
+    if ((rc = dev_alloc(c, sizeof(double) * (size_t)c->CS * S, &p))) return rc;
     c->d_coef = (double*)p;
-    c->d_z = c->d_coef + (kMaxKrylovCap + 2);
-    const int nb = reduction_blocks(N > (long long)c->Mn + c->Ne ? N : (long long)c->Mn + c->Ne);
+    CK(cudaMemset(c->d_coef, 0, sizeof(double) * (size_t)c->CS * S));
+    if ((rc = dev_alloc(c, sizeof(int) * 2 * (size_t)S, &p))) return rc;
+    c->d_mint = (int*)p;
+    if ((rc = dev_alloc(c, sizeof(unsigned int) * (size_t)(S + 3), &p))) return rc;
+    c->d_counters = (unsigned int*)p;
+    CK(cudaMemset(c->d_counters, 0, sizeof(unsigned int) * (size_t)(S + 3)));
+    c->rw.counter = c->d_counters;
+    if ((rc = make_seg(c, c->scen_start, &c->seg))) return rc;
+    std::vector<long long> tstart((size_t)S + 1);
+    for (int s = 0; s <= S; ++s) tstart[s] = (long long)s * ((c->Mn + c->Ne) / S);
+    if ((rc = make_seg(c, tstart, &c->seg_terms))) return rc;
+    const int nb = std::max(std::max(c->seg.nblocks, c->seg_terms.nblocks),
+                            reduction_blocks(std::max(N, (long long)c->Mn + c->Ne)));
     if ((rc = dev_alloc(c, sizeof(double) * (size_t)nb, &p))) return rc;
     c->rw.partials = (double*)p;
-    if ((rc = dev_alloc(c, sizeof(unsigned int) * 4, &p))) return rc;
-    c->rw.counter = (unsigned int*)p;
-    CK(cudaMemset(c->rw.counter, 0, sizeof(unsigned int) * 4));
-    CK(cudaMallocHost(&c->h_scal, sizeof(double) * nscal));
-    CK(cudaMallocHost(&c->h_coef, sizeof(double) * 2 * (kMaxKrylovCap + 2)));
-    CK(cudaMallocHost(&c->h_flag, sizeof(int) * 4));
-    CK(cudaMallocHost(&c->h_eps, sizeof(double) * 2));
-    c->u_base = c->d_u;
-    for (int par = 0; par < 2; ++par) {
-        c->graphs[par].assign((size_t)(maxk > 0 ? maxk : 1), nullptr);
-        c->graph_ev[par].resize((size_t)(maxk > 0 ? maxk : 1));
-        for (auto& a : c->graph_ev[par]) a.fill(nullptr);
+    CK(cudaMallocHost(&c->h_scal, sizeof(double) * (size_t)c->ldH * 2));
+    CK(cudaMallocHost(&c->h_coef, sizeof(double) * (size_t)c->CS * S));
+    CK(cudaMallocHost(&c->h_flag, sizeof(int) * (size_t)S));
+    CK(cudaMallocHost(&c->h_eps, sizeof(double) * 3 * (size_t)S));
+    CK(cudaMallocHost(&c->h_active, sizeof(int) * (size_t)S));
+    CK(cudaMallocHost(&c->h_mint, sizeof(int) * 2 * (size_t)S));
+    CK(cudaMallocHost(&c->h_stage, sizeof(double) * (size_t)(c->ldH + 2) * S));
+    std::memset(c->h_eps, 0, sizeof(double) * 3 * (size_t)S);
+    std::memset(c->h_coef, 0, sizeof(double) * (size_t)c->CS * S);
+    std::memset(c->h_mint, 0, sizeof(int) * 2 * (size_t)S);
+    c->active_now.assign((size_t)S, 0);
+    c->graphs.assign((size_t)mk1, nullptr);
+    c->graph_ev.resize((size_t)mk1);
+    for (auto& a : c->graph_ev) a.fill(nullptr);
+    c->sc.assign((size_t)S, ScenState{});
+    for (auto& q : c->sc) {
+        q.Hm.assign((size_t)c->ldH * mk1, 0.0);
+        q.phi.assign((size_t)mk1 * mk1, 0.0);
+        q.cv.assign((size_t)mk1 + 1, 0.0);
+        q.z.assign((size_t)mk1 + 2, 0.0);
     }
-    c->Hm.assign((size_t)c->ldH * (size_t)(maxk > 0 ? maxk : 1), 0.0);
-    c->phi.assign((size_t)(maxk > 0 ? maxk : 1) * (size_t)(maxk > 0 ? maxk : 1), 0.0);
     return TSR_OK;
 }
 
-int read_flag(tsr_ctx* c, int* flag)
+// per-scenario non-finite flags of the last G launches
+int read_flags(tsr_ctx* c)
 {
-    CK(cudaMemcpyAsync(c->h_flag, c->P.flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(c->h_flag, c->P.flag, sizeof(int) * (size_t)c->S, cudaMemcpyDeviceToHost,
+                       c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    *flag = c->h_flag[0];
     return TSR_OK;
 }
 
 int reset_flag(tsr_ctx* c)
 {
-    CK(cudaMemsetAsync(c->P.flag, 0, sizeof(int), c->stream));
+    CK(cudaMemsetAsync(c->P.flag, 0, sizeof(int) * (size_t)c->S, c->stream));
     return TSR_OK;
+}
+
+double* scal_slot(tsr_ctx* c, int slot, int scen = 0)
+{
+    return c->d_scal + (size_t)c->HS * (size_t)scen + (size_t)c->ldH * (size_t)(c->maxk > 0 ? c->maxk : 1) +
+           slot;
 }
 
 int fetch_scalar(tsr_ctx* c, int slot, double* out)
 {
-    double* base = c->d_scal + (size_t)c->ldH * (size_t)(c->maxk > 0 ? c->maxk : 1);
-    CK(cudaMemcpyAsync(c->h_scal, base + slot, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(c->h_scal, scal_slot(c, slot), sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     *out = c->h_scal[0];
     return TSR_OK;
 }
 
-double* scal_slot(tsr_ctx* c, int slot)
+// slot `slot` of every scenario into out[S]
+int fetch_scalars(tsr_ctx* c, int slot, double* out)
 {
-    return c->d_scal + (size_t)c->ldH * (size_t)(c->maxk > 0 ? c->maxk : 1) + slot;
+    CK(cudaMemcpy2DAsync(c->h_stage, sizeof(double), scal_slot(c, slot), sizeof(double) * (size_t)c->HS,
+                         sizeof(double), (size_t)c->S, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    std::memcpy(out, c->h_stage, sizeof(double) * (size_t)c->S);
+    return TSR_OK;
 }
 
-// device copy of {eps, 1/eps} for the finite-difference kernels
+// the scenario mask of the next launches (no copy when unchanged)
+int set_active(tsr_ctx* c, const std::vector<int>& on)
+{
+    if (c->S == 1 || on == c->active_now) return TSR_OK;
+    CK(cudaStreamSynchronize(c->stream));   // the staging buffer may still be in flight
+    for (int s = 0; s < c->S; ++s) c->h_active[s] = on[s];
+    CK(cudaMemcpyAsync(c->d_active, c->h_active, sizeof(int) * (size_t)c->S, cudaMemcpyHostToDevice,
+                       c->stream));
+    c->active_now = on;
+    return TSR_OK;
+}
+
+// every scenario active (the G, Jv and water entry points work on all)
+int all_active(tsr_ctx* c) { return set_active(c, std::vector<int>((size_t)c->S, 1)); }
+
+// {eps, 1/eps, 1/beta} of every scenario into its scalar slots
+// (the caller has synchronised the stream before writing h_eps)
+int upload_eps(tsr_ctx* c)
+{
+    CK(cudaMemcpy2DAsync(scal_slot(c, S_EPS), sizeof(double) * (size_t)c->HS, c->h_eps, 3 * sizeof(double),
+                         3 * sizeof(double), (size_t)c->S, cudaMemcpyHostToDevice, c->stream));
+    return TSR_OK;
+}
+
+// one finite-difference step for every scenario
 int set_eps(tsr_ctx* c, double eps)
 {
-    CK(cudaStreamSynchronize(c->stream));   // the staging buffer may still be in flight
-    c->h_eps[0] = eps;
-    c->h_eps[1] = 1.0 / eps;
-    CK(cudaMemcpyAsync(scal_slot(c, S_EPS), c->h_eps, 2 * sizeof(double), cudaMemcpyHostToDevice,
-                       c->stream));
-    return TSR_OK;
+    CK(cudaStreamSynchronize(c->stream));
+    for (int s = 0; s < c->S; ++s) {
+        c->h_eps[3 * s] = eps;
+        c->h_eps[3 * s + 1] = 1.0 / eps;
+        c->h_eps[3 * s + 2] = 0.0;
+    }
+    return upload_eps(c);
 }
 
 constexpr size_t kProfMax = 16384;
@@ -683,14 +841,15 @@ extern "C" void tsr_free(tsr_ctx* c)
     }
     for (auto& e : c->marks)
         if (e) cudaEventDestroy(e);
-    for (int par = 0; par < 2; ++par) {
-        for (auto& g : c->graphs[par])
-            if (g) cudaGraphExecDestroy(g);
-        for (auto& a : c->graph_ev[par])
-            for (auto& e : a)
-                if (e) cudaEventDestroy(e);
-    }
+    for (auto& g : c->graphs)
+        if (g) cudaGraphExecDestroy(g);
+    for (auto& a : c->graph_ev)
+        for (auto& e : a)
+            if (e) cudaEventDestroy(e);
     if (c->h_eps) cudaFreeHost(c->h_eps);
+    if (c->h_active) cudaFreeHost(c->h_active);
+    if (c->h_mint) cudaFreeHost(c->h_mint);
+    if (c->h_stage) cudaFreeHost(c->h_stage);
     for (void* p : c->allocs) cudaFree(p);
     if (c->h_scal) cudaFreeHost(c->h_scal);
     if (c->h_coef) cudaFreeHost(c->h_coef);
@@ -705,6 +864,8 @@ extern "C" int tsr_num_unknowns(tsr_ctx* c) { return c ? (int)c->N : 0; }
 extern "C" int tsr_g_eval_device(tsr_ctx* c, const double* d_u, double* d_g)
 {
     if (!c || !d_u || !d_g) return TSR_ERR_ARG;
+    int rc = all_active(c);
+    if (rc) return rc;
     launch_g(c->P, 0, d_u, nullptr, nullptr, nullptr, d_g, c->stream);
     CK(cudaGetLastError());
     return TSR_OK;
@@ -715,6 +876,7 @@ extern "C" int tsr_jv_device(tsr_ctx* c, const double* d_u, const double* d_g0, 
 {
     if (!c || !d_u || !d_g0 || !d_v || !d_w || !(eps != 0.0)) return TSR_ERR_ARG;
     int rc = set_eps(c, eps);
+    if (rc == TSR_OK) rc = all_active(c);
     if (rc) return rc;
     launch_g(c->P, 1, d_u, d_v, d_g0, scal_slot(c, S_EPS), d_w, c->stream);
     CK(cudaGetLastError());
@@ -726,17 +888,18 @@ extern "C" int tsr_g_eval(tsr_ctx* c, const double* u, double* g)
     if (!c || !u || !g) return TSR_ERR_ARG;
     const size_t bytes = sizeof(double) * (size_t)c->N;
     int rc;
+    if ((rc = all_active(c))) return rc;
     if ((rc = reset_flag(c))) return rc;
     CK(cudaMemcpyAsync(c->d_x, u, bytes, cudaMemcpyHostToDevice, c->stream));
     launch_g(c->P, 0, c->d_x, nullptr, nullptr, nullptr, c->d_y, c->stream);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(g, c->d_y, bytes, cudaMemcpyDeviceToHost, c->stream));
-    int flag = 0;
-    if ((rc = read_flag(c, &flag))) return rc;
-    if (flag) {
-        set_error("G: non-finite value");
-        return TSR_ERR_NAN;
-    }
+    if ((rc = read_flags(c))) return rc;
+    for (int q = 0; q < c->S; ++q)
+        if (c->h_flag[q]) {
+            set_error("G: non-finite value");
+            return TSR_ERR_NAN;
+        }
     return TSR_OK;
 }
 
@@ -749,6 +912,7 @@ extern "C" int tsr_jv(tsr_ctx* c, const double* u, const double* g0, const doubl
     CK(cudaMemcpyAsync(c->d_w, v, bytes, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(c->d_g1, g0, bytes, cudaMemcpyHostToDevice, c->stream));
     int rc = set_eps(c, eps);
+    if (rc == TSR_OK) rc = all_active(c);
     if (rc) return rc;
     launch_g(c->P, 1, c->d_x, c->d_w, c->d_g1, scal_slot(c, S_EPS), c->d_y, c->stream);
     CK(cudaGetLastError());
@@ -761,9 +925,34 @@ extern "C" int tsr_water_content(tsr_ctx* c, const double* u, double* water)
 {
     if (!c || !u || !water) return TSR_ERR_ARG;
     CK(cudaMemcpyAsync(c->d_x, u, sizeof(double) * (size_t)c->N, cudaMemcpyHostToDevice, c->stream));
-    launch_water(c->P, c->d_x, c->d_terms, scal_slot(c, S_WATER), c->rw, c->stream);
+    launch_water_terms(c->P, c->d_x, c->d_terms, c->stream);
+    launch_vsum(c->d_terms, single_segment((long long)c->Mn + c->Ne, c->rw), scal_slot(c, S_WATER), 1,
+                c->rw.partials, c->stream);
     CK(cudaGetLastError());
     return fetch_scalar(c, S_WATER, water);
+}
+
+extern "C" int tsr_ensemble_water(tsr_ctx* c, const double* u, double* water)
+{
+    if (!c || !u || !water) return TSR_ERR_ARG;
+    int rc;
+    if ((rc = set_active(c, std::vector<int>((size_t)c->S, 1)))) return rc;
+    CK(cudaMemcpyAsync(c->d_x, u, sizeof(double) * (size_t)c->N, cudaMemcpyHostToDevice, c->stream));
+    launch_water_terms(c->P, c->d_x, c->d_terms, c->stream);
+    // per-scenario sums, scenario s into its S_WATER slot
+    launch_vsum(c->d_terms, c->seg_terms, scal_slot(c, S_WATER), (int)c->HS, c->rw.partials, c->stream);
+    CK(cudaGetLastError());
+    return fetch_scalars(c, S_WATER, water);
+}
+
+extern "C" int tsr_num_scenarios(tsr_ctx* c) { return c ? c->S : 0; }
+
+extern "C" int tsr_scenario_range(tsr_ctx* c, int s, long long* first, long long* count)
+{
+    if (!c || s < 0 || s >= c->S || !first || !count) return TSR_ERR_ARG;
+    *first = c->scen_start[s];
+    *count = c->scen_start[(size_t)s + 1] - c->scen_start[s];
+    return TSR_OK;
 }
 
 extern "C" int tsr_dot(tsr_ctx* c, const double* x, const double* y, int n, double* out)
@@ -772,14 +961,19 @@ extern "C" int tsr_dot(tsr_ctx* c, const double* x, const double* y, int n, doub
     const size_t bytes = sizeof(double) * (size_t)n;
     CK(cudaMemcpyAsync(c->d_x, x, bytes, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(c->d_y, y, bytes, cudaMemcpyHostToDevice, c->stream));
-    launch_dot(c->d_x, c->d_y, n, scal_slot(c, S_DOT), c->rw, c->stream);
+    launch_dot(c->d_x, c->d_y, single_segment(n, c->rw), scal_slot(c, S_DOT), 1, c->rw.partials, c->stream);
     CK(cudaGetLastError());
     return fetch_scalar(c, S_DOT, out);
 }
 
 // ---- EXPREM ------------------------------------------------------------------
 // The same algorithm, operation for operation, as the oracle's
-// oracle_exprem_step: see the description there and in the design notes.
+// oracle_exprem_step (reference src/exprem.cpp), run for the S scenarios of
+// a context in lockstep: each launch covers the scenarios that need it (a
+// device mask), every reduction is segmented per scenario in the
+// single-problem order, and each scenario keeps its own step size, Krylov
+// dimension and statistics.  With one scenario this is the reference's
+// one-step exprem.
 
 extern "C" int tsr_exprem_load(tsr_ctx* c, const double* u_host, double t)
 {
@@ -787,15 +981,33 @@ extern "C" int tsr_exprem_load(tsr_ctx* c, const double* u_host, double t)
     CK(cudaMemcpyAsync(c->d_u, u_host, sizeof(double) * (size_t)c->N, cudaMemcpyHostToDevice,
                        c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    c->state_loaded = true;
-    c->t_state = t;
-    c->g0_valid = false;
+    for (auto& q : c->sc) {
+        q.loaded = true;
+        q.t = t;
+        q.g0_valid = false;
+        q.status = TSR_OK;
+    }
+    return TSR_OK;
+}
+
+extern "C" int tsr_ensemble_load(tsr_ctx* c, const double* u_host, const double* t)
+{
+    if (!c || !u_host || !t) return TSR_ERR_ARG;
+    CK(cudaMemcpyAsync(c->d_u, u_host, sizeof(double) * (size_t)c->N, cudaMemcpyHostToDevice,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int q = 0; q < c->S; ++q) {
+        ScenState& z = c->sc[q];
+        z.loaded = true;
+        z.t = t[q];
+        z.g0_valid = false;
+    }
     return TSR_OK;
 }
 
 extern "C" int tsr_exprem_store(tsr_ctx* c, double* u_host)
 {
-    if (!c || !u_host || !c->state_loaded) return TSR_ERR_ARG;
+    if (!c || !u_host || !c->sc[0].loaded) return TSR_ERR_ARG;
     CK(cudaMemcpyAsync(u_host, c->d_u, sizeof(double) * (size_t)c->N, cudaMemcpyDeviceToHost,
                        c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -804,146 +1016,186 @@ extern "C" int tsr_exprem_store(tsr_ctx* c, double* u_host)
 
 namespace {
 
-int upload_coef(tsr_ctx* c, const double* v, int n, double* dst)
+int phi_host(tsr_ctx* c, ScenState& z, double alpha, int m)
 {
-    std::memcpy(c->h_coef, v, sizeof(double) * (size_t)n);
-    CK(cudaMemcpyAsync(dst, c->h_coef, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
-    // the pinned staging buffer is reused by the next upload: wait for it
-    CK(cudaStreamSynchronize(c->stream));
-    return TSR_OK;
-}
-
-int phi_host(tsr_ctx* c, double alpha, int m)
-{
-    int rc = phipade_host(c->phi.data(), c->Hm.data(), alpha, m, c->ldH, c->maxk);
+    int rc = phipade_host(z.phi.data(), z.Hm.data(), alpha, m, c->ldH, c->maxk);
     if (rc) set_error("phipade: singular Pade denominator");
     return rc;
 }
 
-}  // namespace
-
-namespace {
-
-// The kernels of Arnoldi step j: w = J v_j (finite differences), modified
-// Gram-Schmidt against v_0..v_j, h_{j+1,j} = ||w||, v_{j+1} = w / h_{j+1,j}
-// and the weighted norm of v_{j+1}.  ev (4 events or null) brackets the Jv
-// and the Gram-Schmidt block; otherwise the profiling pool does.
-void arnoldi_kernels(tsr_ctx* c, int j, cudaEvent_t* ev)
+// The kernels of Arnoldi step j for every active scenario: w = J v_j
+// (finite differences), modified Gram-Schmidt against v_0..v_j,
+// h_{j+1,j} = ||w||, v_{j+1} = w / h_{j+1,j} and the weighted norm of
+// v_{j+1}.  ev (4 events or null) brackets the Jv and the Gram-Schmidt
+// block; otherwise the profiling pool does.  j + 6 kernels.
+void arnoldi_kernels(tsr_ctx* c, int j, cudaEvent_t* ev, double frac)
 {
     const long long N = c->N;
     cudaStream_t s = c->stream;
     double* V = c->d_V;
-    double* Hc = c->d_scal + (size_t)j * c->ldH;
+    const int HS = (int)c->HS;
+    double* Hc = c->d_scal + (size_t)j * c->ldH;   // scenario q's column at Hc + q HS
+    const SegInfo& g = c->seg;
+    double* part = c->rw.partials;
     int pe = -1;
     // inside a capture, only "external" records become event-record nodes
     if (ev) cudaEventRecordWithFlags(ev[0], s, cudaEventRecordExternal);
-    else pe = prof_begin(c, 0, g_bytes(c, true));
+    else pe = prof_begin(c, 0, frac * g_bytes(c, true));
     launch_g(c->P, 1, c->d_u, V + (size_t)j * N, c->d_g0, scal_slot(c, S_EPS), c->d_w, s);
     if (ev) {
         cudaEventRecordWithFlags(ev[1], s, cudaEventRecordExternal);
         cudaEventRecordWithFlags(ev[2], s, cudaEventRecordExternal);
     } else {
         prof_end(c, pe);
-        pe = prof_begin(c, 1, 8.0 * (double)N * (double)(j + 3));   // algorithmic minimum
+        pe = prof_begin(c, 1, frac * 8.0 * (double)N * (double)(j + 3));   // algorithmic minimum
     }
-    launch_dot(c->d_w, V, N, Hc, c->rw, s);
+    launch_dot(c->d_w, V, g, Hc, HS, part, s);
     for (int i = 0; i <= j; ++i) {
         const double* vnext = (i < j) ? V + (size_t)(i + 1) * N : nullptr;
         double* res = (i < j) ? Hc + i + 1 : scal_slot(c, S_HSQ);
-        launch_mgs(c->d_w, V + (size_t)i * N, Hc + i, vnext, N, res, c->rw, s);
+        launch_mgs(c->d_w, V + (size_t)i * N, Hc + i, HS, vnext, g, res, HS, part, s);
     }
-    launch_scale_wsq(c->d_w, scal_slot(c, S_HSQ), Hc + j + 1, scal_slot(c, S_IH),
-                     V + (size_t)(j + 1) * N, c->d_winv, N, scal_slot(c, S_SV), c->rw, s);
+    launch_scale_wsq(c->d_w, scal_slot(c, S_HSQ), Hc + j + 1, scal_slot(c, S_IH), HS,
+                     V + (size_t)(j + 1) * N, c->d_winv, g, scal_slot(c, S_SV), part, s);
     if (ev) cudaEventRecordWithFlags(ev[3], s, cudaEventRecordExternal);
     else prof_end(c, pe);
 }
 
-}  // namespace
+struct RoundIO {
+    double tend;
+    const double* tspan;
+    double* const* solns;              // [S] rows of tspan solutions, or null
+    const exprem_options_struct* opt;
+    exprem_stats_struct* st;           // [S]
+};
 
-extern "C" int tsr_exprem_advance(tsr_ctx* c, double tend, const double* tspan, double* tspan_solns,
-                                  const exprem_options_struct* opt, exprem_stats_struct* st,
-                                  double* t_out)
+// One accepted step for every scenario of `part`.  A scenario that fails
+// records its status and leaves the round; a CUDA error ends the round.
+int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
 {
-    if (!c || !opt || !st || !tspan || !c->state_loaded) return TSR_ERR_ARG;
-    if (c->maxk < 1) {
-        set_error("context created without a Krylov basis (max_krylov = 0)");
-        return TSR_ERR_ARG;
-    }
-    const long long N = c->N;
-    const size_t bytes = sizeof(double) * (size_t)N;
-    int maxk = opt->MaxKrylov < (int)N ? opt->MaxKrylov : (int)N;
-    if (maxk > c->maxk) maxk = c->maxk;
-    const int ldH = c->ldH;
-    double t = c->t_state;
-    if (t == 0.0) {
-        st->NumSteps = 0;
-        st->FuncEvals = 0;
-        st->CurrentStep = opt->InitStep;
-        st->CurrentKryDim = 0;
-        st->CurrentTime = 0.0;
-        c->g0_valid = false;
-    }
-    if (st->NumSteps >= opt->MaxNumSteps) {
-        set_error("MaxNumSteps reached");
-        return TSR_ERR_MAXSTEPS;
-    }
-    double dt = st->CurrentStep;
-    if (dt > opt->MaxStep) dt = opt->MaxStep;
-    bool last = false;
-    if (t + dt >= tend) {
-        dt = tend - t;
-        last = true;
-    }
-    int rc;
+    const int S = c->S;
+    const exprem_options_struct* opt = io.opt;
     cudaStream_t s = c->stream;
+    const long long N = c->N;
     double* V = c->d_V;
-    double* Hd = c->d_scal;   // Hessenberg block, column j at j*ldH
-    if (!c->g0_valid) {
+    const int ldH = c->ldH;
+    const int HS = (int)c->HS;
+    const int mk1 = c->maxk > 0 ? c->maxk : 1;
+    int rc;
+    auto Ns = [&](int q) { return c->scen_start[(size_t)q + 1] - c->scen_start[q]; };
+    auto fail = [&](int q, int code, const char* msg) {
+        c->sc[q].status = code;
+        set_error(msg);
+    };
+    auto mask_of = [&](const std::vector<int>& set) {
+        std::vector<int> m((size_t)S, 0);
+        for (int q : set) m[q] = 1;
+        return m;
+    };
+    // step set-up
+    std::vector<int> live;
+    for (int q : part) {
+        ScenState& z = c->sc[q];
+        exprem_stats_struct& st = io.st[q];
+        z.status = TSR_OK;
+        if (z.t == 0.0) {
+            st.NumSteps = 0;
+            st.FuncEvals = 0;
+            st.CurrentStep = opt->InitStep;
+            st.CurrentKryDim = 0;
+            st.CurrentTime = 0.0;
+            z.g0_valid = false;
+        }
+        if (st.NumSteps >= opt->MaxNumSteps) {
+            fail(q, TSR_ERR_MAXSTEPS, "MaxNumSteps reached");
+            continue;
+        }
+        long long mq = std::min((long long)opt->MaxKrylov, Ns(q));
+        z.maxk = (int)std::min(mq, (long long)c->maxk);
+        z.dt = st.CurrentStep;
+        if (z.dt > opt->MaxStep) z.dt = opt->MaxStep;
+        z.last = false;
+        if (z.t + z.dt >= io.tend) {
+            z.dt = io.tend - z.t;
+            z.last = true;
+        }
+        live.push_back(q);
+    }
+    // G(u) where the previous step did not leave it
+    std::vector<int> need;
+    for (int q : live)
+        if (!c->sc[q].g0_valid) need.push_back(q);
+    if (!need.empty()) {
+        if ((rc = set_active(c, mask_of(need)))) return rc;
         if ((rc = reset_flag(c))) return rc;
-        int pe = prof_begin(c, 0, g_bytes(c, false));
+        int pe = prof_begin(c, 0, g_bytes(c, false) * need.size() / S);
         launch_g(c->P, 0, c->d_u, nullptr, nullptr, nullptr, c->d_g0, s);
         prof_end(c, pe);
         CK(cudaGetLastError());
-        st->FuncEvals++;
-        int flag = 0;
-        if ((rc = read_flag(c, &flag))) return rc;
-        if (flag) {
-            set_error("G(u) non-finite at the current state");
-            return TSR_ERR_GFUNC;
+        if ((rc = read_flags(c))) return rc;
+        std::vector<int> keep;
+        for (int q : live) {
+            ScenState& z = c->sc[q];
+            if (!z.g0_valid) {
+                io.st[q].FuncEvals++;
+                if (c->h_flag[q]) {
+                    fail(q, TSR_ERR_GFUNC, "G(u) non-finite at the current state");
+                    continue;
+                }
+                z.g0_valid = true;
+            }
+            keep.push_back(q);
         }
-        c->g0_valid = true;
+        live.swap(keep);
     }
-    std::fill(c->Hm.begin(), c->Hm.end(), 0.0);
-    launch_winv(c->d_u, opt->RelTol, opt->AbsTol, c->d_winv, N, s);
-    launch_dot(c->d_g0, c->d_g0, N, scal_slot(c, S_BETA2), c->rw, s);
-    launch_dot(c->d_u, c->d_u, N, scal_slot(c, S_NU2), c->rw, s);
+    if (live.empty()) return TSR_OK;
+    if ((rc = set_active(c, mask_of(live)))) return rc;
+    launch_winv(c->d_u, opt->RelTol, opt->AbsTol, c->d_winv, c->seg, s);
+    launch_dot(c->d_g0, c->d_g0, c->seg, scal_slot(c, S_BETA2), HS, c->rw.partials, s);
+    launch_dot(c->d_u, c->d_u, c->seg, scal_slot(c, S_NU2), HS, c->rw.partials, s);
     CK(cudaGetLastError());
-    double b2, n2;
-    if ((rc = fetch_scalar(c, S_BETA2, &b2))) return rc;
-    if ((rc = fetch_scalar(c, S_NU2, &n2))) return rc;
-    const double beta = std::sqrt(b2);
-    const double nu = std::sqrt(n2);
-    const double eps = std::sqrt((1.0 + nu) * DBL_EPSILON);
-    int m = 0;
-    bool happy = false;
-    double errK = 0.0, vnw = 0.0;
-    if (beta != 0.0) {
-        const double ib = 1.0 / beta;
-        launch_scale(c->d_g0, ib, V, N, s);
-        if ((rc = set_eps(c, eps))) return rc;
-        const int par = (c->d_u == c->u_base) ? 0 : 1;
-        for (int j = 0; j < maxk; ++j) {
-            double* Hc = Hd + (size_t)j * ldH;
-            double* vn = V + (size_t)(j + 1) * N;
+    static_assert(S_NU2 == S_BETA2 + 1, "beta^2 and |u|^2 are fetched together");
+    CK(cudaMemcpy2DAsync(c->h_stage, 2 * sizeof(double), scal_slot(c, S_BETA2), sizeof(double) * HS,
+                         2 * sizeof(double), (size_t)S, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    std::vector<int> arn((size_t)S, 0);
+    int narn = 0;
+    for (int q : live) {
+        ScenState& z = c->sc[q];
+        std::fill(z.Hm.begin(), z.Hm.end(), 0.0);
+        z.beta = std::sqrt(c->h_stage[2 * q]);
+        z.nu = std::sqrt(c->h_stage[2 * q + 1]);
+        z.eps = std::sqrt((1.0 + z.nu) * DBL_EPSILON);
+        z.m = 0;
+        z.happy = false;
+        z.errK = 0.0;
+        z.vnw = 0.0;
+        z.iterating = z.beta != 0.0;
+        c->h_eps[3 * q] = z.eps;
+        c->h_eps[3 * q + 1] = 1.0 / z.eps;
+        c->h_eps[3 * q + 2] = z.iterating ? 1.0 / z.beta : 0.0;
+        if (z.iterating) {
+            arn[q] = 1;
+            ++narn;
+        }
+    }
+    // Arnoldi, all iterating scenarios together
+    if (narn > 0) {
+        if ((rc = upload_eps(c))) return rc;
+        if ((rc = set_active(c, arn))) return rc;
+        launch_seg_scale(c->d_g0, scal_slot(c, S_IB), HS, V, c->seg, s);
+        for (int j = 0; j < c->maxk && narn > 0; ++j) {
+            if ((rc = set_active(c, arn))) return rc;
+            const double frac = (double)narn / S;
             if (c->use_graphs) {
-                cudaGraphExec_t& ge = c->graphs[par][(size_t)j];
-                std::array<cudaEvent_t, 4>& ev = c->graph_ev[par][(size_t)j];
+                cudaGraphExec_t& ge = c->graphs[(size_t)j];
+                std::array<cudaEvent_t, 4>& ev = c->graph_ev[(size_t)j];
                 if (!ge) {
                     for (auto& e : ev)
                         if (!e) CK(cudaEventCreate(&e));
                     set_counting(false);
                     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-                    arnoldi_kernels(c, j, ev.data());
+                    arnoldi_kernels(c, j, ev.data(), frac);
                     cudaGraph_t g = nullptr;
                     cudaError_t ce = cudaStreamEndCapture(s, &g);
                     set_counting(true);
@@ -954,149 +1206,270 @@ extern "C" int tsr_exprem_advance(tsr_ctx* c, double tend, const double* tspan, 
                 CK(cudaGraphLaunch(ge, s));
                 add_launches(j + 6);
             } else {
-                arnoldi_kernels(c, j, nullptr);
+                arnoldi_kernels(c, j, nullptr, frac);
             }
-            st->FuncEvals++;
+            for (int q = 0; q < S; ++q)
+                if (arn[q]) io.st[q].FuncEvals++;
             CK(cudaGetLastError());
-            // column j of H and the weighted norm of v_{j+1}
-            CK(cudaMemcpyAsync(c->h_scal, Hc, sizeof(double) * (size_t)(j + 2), cudaMemcpyDeviceToHost, s));
-            CK(cudaMemcpyAsync(c->h_scal + ldH, scal_slot(c, S_SV), sizeof(double), cudaMemcpyDeviceToHost, s));
+            // column j of every H and the weighted norms of v_{j+1}
+            const size_t row = (size_t)ldH + 1;
+            CK(cudaMemcpy2DAsync(c->h_stage, sizeof(double) * row, c->d_scal + (size_t)j * ldH,
+                                 sizeof(double) * HS, sizeof(double) * (size_t)(j + 2), (size_t)S,
+                                 cudaMemcpyDeviceToHost, s));
+            CK(cudaMemcpy2DAsync(c->h_stage + ldH, sizeof(double) * row, scal_slot(c, S_SV),
+                                 sizeof(double) * HS, sizeof(double), (size_t)S, cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
             if (c->use_graphs && c->prof) {
-                std::array<cudaEvent_t, 4>& ev = c->graph_ev[par][(size_t)j];
-                float a = 0.f, b = 0.f;
-                CK(cudaEventElapsedTime(&a, ev[0], ev[1]));
-                CK(cudaEventElapsedTime(&b, ev[2], ev[3]));
-                c->prof_acc_ms[0] += a;
-                c->prof_acc_bytes[0] += g_bytes(c, true);
+                std::array<cudaEvent_t, 4>& ev = c->graph_ev[(size_t)j];
+                float ta = 0.f, tb = 0.f;
+                CK(cudaEventElapsedTime(&ta, ev[0], ev[1]));
+                CK(cudaEventElapsedTime(&tb, ev[2], ev[3]));
+                c->prof_acc_ms[0] += ta;
+                c->prof_acc_bytes[0] += frac * g_bytes(c, true);
                 c->prof_acc_n[0] += 1;
-                c->prof_acc_ms[1] += b;
-                c->prof_acc_bytes[1] += 8.0 * (double)N * (double)(j + 3);
+                c->prof_acc_ms[1] += tb;
+                c->prof_acc_bytes[1] += frac * 8.0 * (double)N * (double)(j + 3);
                 c->prof_acc_n[1] += 1;
             }
-            double hs = 0.0;
-            for (int i = 0; i <= j; ++i) {
-                const double hij = c->h_scal[i];
-                c->Hm[(size_t)j * ldH + i] = hij;
-                hs = std::fma(hij, hij, hs);
+            for (int q = 0; q < S; ++q) {
+                if (!arn[q]) continue;
+                ScenState& z = c->sc[q];
+                const double* col = c->h_stage + (size_t)q * row;
+                double hs = 0.0;
+                for (int i = 0; i <= j; ++i) {
+                    z.Hm[(size_t)j * ldH + i] = col[i];
+                    hs = std::fma(col[i], col[i], hs);
+                }
+                const double hn = col[j + 1];
+                z.Hm[(size_t)j * ldH + j + 1] = hn;
+                const double Sv = col[ldH];
+                z.m = j + 1;
+                bool stop = false;
+                if (!(hn > 1e-12 * std::sqrt(std::fma(hn, hn, hs)))) {
+                    z.happy = true;
+                    stop = true;
+                } else if (!(z.m < opt->MinKrylov && z.m < z.maxk)) {
+                    z.vnw = std::sqrt(Sv / (double)Ns(q));
+                    if ((rc = phi_host(c, z, z.dt, z.m))) {
+                        fail(q, rc, "phipade: singular Pade denominator");
+                        stop = true;
+                    } else {
+                        z.errK = std::fabs(((z.dt * z.beta) * hn) * z.phi[(size_t)z.m - 1]) * z.vnw;
+                        if (z.errK <= kKrylovTol) stop = true;
+                    }
+                }
+                if (z.m >= z.maxk) stop = true;
+                if (stop) {
+                    arn[q] = 0;
+                    --narn;
+                }
             }
-            const double hn = c->h_scal[j + 1];
-            c->Hm[(size_t)j * ldH + j + 1] = hn;
-            const double Sv = c->h_scal[ldH];
-            m = j + 1;
-            if (!(hn > 1e-12 * std::sqrt(std::fma(hn, hn, hs)))) {
-                happy = true;
+        }
+    }
+    // Krylov error too large at the largest dimension: shorten the step
+    for (int q : live) {
+        ScenState& z = c->sc[q];
+        if (z.status || z.beta == 0.0 || z.happy) continue;
+        while (z.errK > kKrylovTol) {
+            const double f = 0.5 > opt->MinStepDecFac ? 0.5 : opt->MinStepDecFac;
+            z.dt = z.dt * f;
+            z.last = false;
+            if (z.dt < opt->MinStep) {
+                fail(q, TSR_ERR_MINSTEP, "step size below MinStep (Krylov)");
                 break;
             }
-            if (m < opt->MinKrylov && m < maxk) continue;
-            vnw = std::sqrt(Sv / (double)N);
-            if ((rc = phi_host(c, dt, m))) return rc;
-            errK = std::fabs(((dt * beta) * hn) * c->phi[m - 1]) * vnw;
-            if (errK <= kKrylovTol) break;
-        }
-        if (!happy && errK > kKrylovTol) {
-            while (errK > kKrylovTol) {
-                const double f = 0.5 > opt->MinStepDecFac ? 0.5 : opt->MinStepDecFac;
-                dt = dt * f;
-                last = false;
-                if (dt < opt->MinStep) {
-                    set_error("step size below MinStep (Krylov)");
-                    return TSR_ERR_MINSTEP;
-                }
-                if ((rc = phi_host(c, dt, m))) return rc;
-                errK = std::fabs(((dt * beta) * c->Hm[(size_t)(m - 1) * ldH + m]) * c->phi[m - 1]) * vnw;
+            if ((rc = phi_host(c, z, z.dt, z.m))) {
+                fail(q, rc, "phipade: singular Pade denominator");
+                break;
             }
+            z.errK = std::fabs(((z.dt * z.beta) * z.Hm[(size_t)(z.m - 1) * ldH + z.m]) *
+                               z.phi[(size_t)z.m - 1]) * z.vnw;
         }
     }
-    std::vector<double> cv((size_t)kMaxKrylovCap + 1), z((size_t)kMaxKrylovCap + 2);
-    for (;;) {
-        if (m > 0) {
-            if ((rc = phi_host(c, dt, m))) return rc;
-            const double dtb = dt * beta;
-            for (int i = 0; i < m; ++i) cv[i] = dtb * c->phi[i];
-            if ((rc = upload_coef(c, cv.data(), m, c->d_coef))) return rc;
-            launch_combine(c->d_u, V, N, c->d_coef, m, c->d_unew, N, s);
-        } else {
-            CK(cudaMemcpyAsync(c->d_unew, c->d_u, bytes, cudaMemcpyDeviceToDevice, s));
+    // step attempts: u_new = u + dt beta V phi_1(dt H) e_1, G(u_new), error
+    std::vector<int> pend;
+    for (int q : live)
+        if (!c->sc[q].status) pend.push_back(q);
+    const int zoff = mk1 + 1, doff = c->CS - 1;
+    std::vector<double> errs((size_t)S);
+    while (!pend.empty()) {
+        CK(cudaStreamSynchronize(s));   // staging buffers may still be in flight
+        std::vector<int> go;
+        for (int q : pend) {
+            ScenState& z = c->sc[q];
+            const int m = z.m;
+            int mz = 0;
+            if (m > 0) {
+                if ((rc = phi_host(c, z, z.dt, m))) {
+                    fail(q, rc, "phipade: singular Pade denominator");
+                    continue;
+                }
+                const double dtb = z.dt * z.beta;
+                for (int i = 0; i < m; ++i) z.cv[i] = dtb * z.phi[i];
+                mz = z.happy ? m : m + 1;
+                for (int i = 0; i < mz; ++i) {
+                    double a = 0.0;
+                    for (int k = 0; k < m; ++k) a = std::fma(z.Hm[(size_t)k * ldH + i], z.cv[k], a);
+                    z.z[i] = a;
+                }
+            }
+            double* cq = c->h_coef + (size_t)q * c->CS;
+            for (int i = 0; i < m; ++i) cq[i] = z.cv[i];
+            for (int i = 0; i < mz; ++i) cq[zoff + i] = z.z[i];
+            cq[doff] = z.dt / 3.0;
+            c->h_mint[q] = m;
+            c->h_mint[S + q] = mz;
+            go.push_back(q);
         }
+        pend.swap(go);
+        if (pend.empty()) break;
+        if ((rc = set_active(c, mask_of(pend)))) return rc;
+        CK(cudaMemcpyAsync(c->d_coef, c->h_coef, sizeof(double) * (size_t)c->CS * S, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(c->d_mint, c->h_mint, sizeof(int) * 2 * (size_t)S, cudaMemcpyHostToDevice, s));
+        launch_combine(c->d_u, V, N, c->d_coef, c->CS, c->d_mint, c->d_unew, c->seg, s);
         if ((rc = reset_flag(c))) return rc;
-        int pe = prof_begin(c, 0, g_bytes(c, false));
+        int pe = prof_begin(c, 0, g_bytes(c, false) * pend.size() / S);
         launch_g(c->P, 0, c->d_unew, nullptr, nullptr, nullptr, c->d_g1, s);
         prof_end(c, pe);
-        st->FuncEvals++;
-        double err = 0.0;
-        int mz = 0;
-        if (m > 0) {
-            mz = happy ? m : m + 1;
-            for (int i = 0; i < mz; ++i) {
-                double a = 0.0;
-                for (int k = 0; k < m; ++k) a = std::fma(c->Hm[(size_t)k * ldH + i], cv[k], a);
-                z[i] = a;
-            }
-            if ((rc = upload_coef(c, z.data(), mz, c->d_z))) return rc;
-            launch_err(c->d_g1, c->d_g0, V, N, c->d_z, mz, dt / 3.0, c->d_winv, N, scal_slot(c, S_ERR),
-                       c->rw, s);
-        }
+        for (int q : pend) io.st[q].FuncEvals++;
+        launch_err(c->d_g1, c->d_g0, V, N, c->d_coef + zoff, c->CS, c->d_mint + S, c->d_coef + doff, c->CS,
+                   c->d_winv, c->seg, scal_slot(c, S_ERR), HS, c->rw.partials, s);
         CK(cudaGetLastError());
-        int flag = 0;
-        if ((rc = read_flag(c, &flag))) return rc;
-        if (flag) {
-            err = INFINITY;
-        } else if (m > 0) {
-            double S;
-            if ((rc = fetch_scalar(c, S_ERR, &S))) return rc;
-            err = std::sqrt(S / (double)N);
-        }
-        if (err <= 1.0) {
-            const int ns = (int)tspan[0];
-            const double tn = last ? tend : t + dt;
-            for (int k = 1; k <= ns; ++k) {
-                if (tspan[k] > t && tspan[k] <= tn && tspan_solns) {
-                    double* row = tspan_solns + (size_t)k * (size_t)N;
-                    if (m == 0) {
-                        CK(cudaMemcpyAsync(row, c->d_u, bytes, cudaMemcpyDeviceToHost, s));
-                    } else {
-                        const double tau = tspan[k] - t;
-                        if ((rc = phi_host(c, tau, m))) return rc;
-                        const double tb = tau * beta;
-                        std::vector<double> cd((size_t)m);
-                        for (int i = 0; i < m; ++i) cd[i] = tb * c->phi[i];
-                        if ((rc = upload_coef(c, cd.data(), m, c->d_coef))) return rc;
-                        launch_combine(c->d_u, V, N, c->d_coef, m, c->d_x, N, s);
-                        CK(cudaMemcpyAsync(row, c->d_x, bytes, cudaMemcpyDeviceToHost, s));
-                    }
-                    CK(cudaStreamSynchronize(s));
-                }
+        if ((rc = read_flags(c))) return rc;
+        if ((rc = fetch_scalars(c, S_ERR, errs.data()))) return rc;
+        std::vector<int> acc, next;
+        for (int q : pend) {
+            ScenState& z = c->sc[q];
+            double err = 0.0;
+            if (c->h_flag[q]) err = INFINITY;
+            else if (z.m > 0) err = std::sqrt(errs[q] / (double)Ns(q));
+            z.err = err;
+            if (err <= 1.0) {
+                acc.push_back(q);
+                continue;
             }
-            std::swap(c->d_u, c->d_unew);
-            std::swap(c->d_g0, c->d_g1);
-            t = tn;
-            double fac = (err > 0.0) ? opt->SafetyFac * std::pow(err, -1.0 / 3.0) : opt->MaxStepIncFac;
+            double fac = (err == err && err < INFINITY) ? opt->SafetyFac * std::pow(err, -1.0 / 3.0)
+                                                         : opt->MinStepDecFac;
+            if (fac < opt->MinStepDecFac) fac = opt->MinStepDecFac;
+            if (fac > 1.0) fac = opt->MinStepDecFac;
+            z.dt = z.dt * fac;
+            z.last = false;
+            if (z.dt < opt->MinStep) {
+                fail(q, TSR_ERR_MINSTEP, "step size below MinStep");
+                continue;
+            }
+            next.push_back(q);
+        }
+        // accepted: solutions at the tspan times inside the step, then the
+        // new state and its G
+        const int ns = (int)io.tspan[0];
+        for (int q : acc) {
+            ScenState& z = c->sc[q];
+            const double tn = z.last ? io.tend : z.t + z.dt;
+            double* rows = io.solns ? io.solns[q] : nullptr;
+            if (!rows) continue;
+            const long long off = c->scen_start[q], n = Ns(q);
+            for (int k = 1; k <= ns; ++k) {
+                if (!(io.tspan[k] > z.t && io.tspan[k] <= tn)) continue;
+                double* row = rows + (size_t)k * (size_t)n;
+                if (z.m == 0) {
+                    CK(cudaMemcpyAsync(row, c->d_u + off, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, s));
+                } else {
+                    const double tau = io.tspan[k] - z.t;
+                    if ((rc = phi_host(c, z, tau, z.m))) {
+                        fail(q, rc, "phipade: singular Pade denominator");
+                        break;
+                    }
+                    const double tb = tau * z.beta;
+                    CK(cudaStreamSynchronize(s));
+                    double* cq = c->h_coef + (size_t)q * c->CS;
+                    for (int i = 0; i < z.m; ++i) cq[i] = tb * z.phi[i];
+                    CK(cudaMemcpyAsync(c->d_coef + (size_t)q * c->CS, cq, sizeof(double) * (size_t)z.m,
+                                       cudaMemcpyHostToDevice, s));
+                    if ((rc = set_active(c, mask_of({q})))) return rc;
+                    launch_combine(c->d_u, V, N, c->d_coef, c->CS, c->d_mint, c->d_x, c->seg, s);
+                    CK(cudaMemcpyAsync(row, c->d_x + off, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, s));
+                }
+                CK(cudaStreamSynchronize(s));
+            }
+        }
+        std::vector<int> ok;
+        for (int q : acc)
+            if (!c->sc[q].status) ok.push_back(q);
+        if (!ok.empty()) {
+            if ((rc = set_active(c, mask_of(ok)))) return rc;
+            launch_seg_copy2(c->d_unew, c->d_u, c->d_g1, c->d_g0, c->seg, s);
+            CK(cudaGetLastError());
+        }
+        for (int q : ok) {
+            ScenState& z = c->sc[q];
+            exprem_stats_struct& st = io.st[q];
+            const double tn = z.last ? io.tend : z.t + z.dt;
+            z.t = tn;
+            double fac = (z.err > 0.0) ? opt->SafetyFac * std::pow(z.err, -1.0 / 3.0) : opt->MaxStepIncFac;
             if (fac > opt->MaxStepIncFac) fac = opt->MaxStepIncFac;
             if (fac < opt->MinStepDecFac) fac = opt->MinStepDecFac;
-            double dn = dt * fac;
+            double dn = z.dt * fac;
             if (dn > opt->MaxStep) dn = opt->MaxStep;
             if (dn < opt->MinStep) dn = opt->MinStep;
-            st->CurrentStep = dn;
-            st->CurrentTime = t;
-            st->CurrentKryDim = m;
-            st->NumSteps++;
-            c->t_state = t;
-            c->g0_valid = true;
-            if (t_out) *t_out = t;
-            return TSR_OK;
+            st.CurrentStep = dn;
+            st.CurrentTime = tn;
+            st.CurrentKryDim = z.m;
+            st.NumSteps++;
+            z.g0_valid = true;
         }
-        double fac = (err == err && err < INFINITY) ? opt->SafetyFac * std::pow(err, -1.0 / 3.0)
-                                                     : opt->MinStepDecFac;
-        if (fac < opt->MinStepDecFac) fac = opt->MinStepDecFac;
-        if (fac > 1.0) fac = opt->MinStepDecFac;
-        dt = dt * fac;
-        last = false;
-        if (dt < opt->MinStep) {
-            set_error("step size below MinStep");
-            return TSR_ERR_MINSTEP;
-        }
+        pend.swap(next);
     }
+    CK(cudaStreamSynchronize(s));
+    return TSR_OK;
+}
+
+}  // namespace
+
+extern "C" int tsr_exprem_advance(tsr_ctx* c, double tend, const double* tspan, double* tspan_solns,
+                                  const exprem_options_struct* opt, exprem_stats_struct* st,
+                                  double* t_out)
+{
+    if (!c || !opt || !st || !tspan || !c->sc[0].loaded) return TSR_ERR_ARG;
+    if (c->S != 1) {
+        set_error("a context of several scenarios advances with tsr_ensemble_advance");
+        return TSR_ERR_ARG;
+    }
+    if (c->maxk < 1) {
+        set_error("context created without a Krylov basis (max_krylov = 0)");
+        return TSR_ERR_ARG;
+    }
+    double* solns[1] = {tspan_solns};
+    RoundIO io{tend, tspan, solns, opt, st};
+    int rc = exprem_round(c, std::vector<int>{0}, io);
+    if (rc) return rc;
+    if (c->sc[0].status) return c->sc[0].status;
+    if (t_out) *t_out = c->sc[0].t;
+    return TSR_OK;
+}
+
+extern "C" int tsr_ensemble_advance(tsr_ctx* c, double tend, const double* tspan, double* const* tspan_solns,
+                                    const exprem_options_struct* opt, exprem_stats_struct* stats,
+                                    double* t, int* status, int* n_running)
+{
+    if (!c || !opt || !stats || !tspan || !t || !status || !c->sc[0].loaded) return TSR_ERR_ARG;
+    if (c->maxk < 1) {
+        set_error("context created without a Krylov basis (max_krylov = 0)");
+        return TSR_ERR_ARG;
+    }
+    std::vector<int> part;
+    for (int q = 0; q < c->S; ++q)
+        if (c->sc[q].status == TSR_OK && c->sc[q].t < tend) part.push_back(q);
+    RoundIO io{tend, tspan, tspan_solns, opt, stats};
+    int rc = part.empty() ? TSR_OK : exprem_round(c, part, io);
+    int run = 0;
+    for (int q = 0; q < c->S; ++q) {
+        t[q] = c->sc[q].t;
+        status[q] = c->sc[q].status;
+        if (status[q] == TSR_OK && t[q] < tend) ++run;
+    }
+    if (n_running) *n_running = run;
+    return rc;
 }
 
 extern "C" int tsr_exprem_step(tsr_ctx* c, double* t, double tend, const double* tspan,
@@ -1106,13 +1479,13 @@ extern "C" int tsr_exprem_step(tsr_ctx* c, double* t, double tend, const double*
     if (!c || !t || !u0 || !opt || !st || !tspan) return TSR_ERR_ARG;
     // reuse G(u) of the previous accepted step when the caller hands back
     // the same state (same array, same time)
-    const bool cached = c->state_loaded && c->g0_valid && c->last_u0 == u0 && c->last_t == *t &&
-                        *t != 0.0;
+    ScenState& z = c->sc[0];
+    const bool cached = z.loaded && z.g0_valid && c->last_u0 == u0 && c->last_t == *t && *t != 0.0;
     int rc;
     if (cached) {
         CK(cudaMemcpyAsync(c->d_u, u0, sizeof(double) * (size_t)c->N, cudaMemcpyHostToDevice,
                            c->stream));
-        c->t_state = *t;
+        z.t = *t;
     } else {
         if ((rc = tsr_exprem_load(c, u0, *t))) return rc;
     }
@@ -1293,6 +1666,8 @@ extern "C" int tsr_autotune(tsr_ctx* c, const double* u_host, int reps, double* 
     if (!c || !u_host) return TSR_ERR_ARG;
     if (reps < 1) reps = 3;
     CK(cudaMemcpyAsync(c->d_x, u_host, sizeof(double) * (size_t)c->N, cudaMemcpyHostToDevice, c->stream));
+    int rc0 = all_active(c);
+    if (rc0) return rc0;
     const int thr[] = {128, 256, 512, 1024};
     const int bud[] = {48 * 1024, 64 * 1024, 96 * 1024, 144 * 1024, 200 * 1024};
     double best = 1e30;

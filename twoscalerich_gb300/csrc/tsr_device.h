@@ -73,6 +73,12 @@ struct MacroDev {
     int model_type;
     double keff_first, keff_inv_logr;
     double epsA, inv_Y, Ss, bflux;
+    // ensemble form: nscen scenarios of scen_nodes nodes and scen_cells cells
+    int nscen, scen_nodes, scen_cells;
+    int pad2;
+    const long long* node_off;          // [Mn] unknown of macro node i, or nullptr (identity)
+    const struct VGPar* scen_pA;        // [nscen] or nullptr (pA)
+    const double* scen_kscale;          // [nscen] or nullptr (1)
 };
 
 struct Problem {
@@ -86,8 +92,25 @@ struct Problem {
     int micro_grid;             // persistent grid of the cell kernel
     int misc_slots;             // per-cell scratch slots reserved in shared memory
     double* contrib;            // [16*Ne] macro contributions per element
-    int* flag;                  // device word: bit 0 non-finite G
+    int* flag;                  // [nscen] device words: bit 0 non-finite G in scenario s
+    const int* active;          // [nscen] scenarios to evaluate, or nullptr (all)
+    int eps_stride;             // doubles between consecutive scenarios' {eps, 1/eps}
     long long N;
+};
+
+// Vector segments (one per scenario) for reductions and elementwise work.
+// Block b of a segmented launch covers items [start_s + 8192 lb, ...) of
+// segment s = blkseg[b], lb = b - block0[s]: chunking is relative to the
+// segment, so each segment is reduced in exactly the order it would be alone.
+struct SegInfo {
+    int nseg;                   // segments
+    int nblocks;                // blocks of a launch over all segments
+    long long n1;               // length when there is one implicit segment
+    const long long* start;     // [nseg+1] or nullptr (one segment [0, n1))
+    const int* block0;          // [nseg+1]
+    const int* blkseg;          // [nblocks]
+    unsigned int* counters;     // [nseg]
+    const int* active;          // [nseg] or nullptr (all)
 };
 
 // Opt the cell kernel into its dynamic shared memory and report how many
@@ -101,30 +124,44 @@ int configure_cell_kernels(const Problem& P, int* occ);
 void launch_g(const Problem& P, int mode, const double* u, const double* v, const double* g0,
               const double* epsv, double* out, cudaStream_t s);
 
-// Fixed-order reductions (result written to device scalar *res).
+// Fixed-order reductions; segment s writes its result to res[s * rstride].
 struct RedWork {
-    double* partials;       // [nblocks]
-    unsigned int* counter;  // one word per concurrent reduction slot
+    double* partials;       // [blocks]
+    unsigned int* counter;  // counters of single-segment launches
 };
 int reduction_blocks(long long n);
-void launch_dot(const double* x, const double* y, long long n, double* res, RedWork w, cudaStream_t s);
-void launch_wsq(const double* x, const double* winv, long long n, double* res, RedWork w, cudaStream_t s);
-void launch_vsum(const double* x, long long n, double* res, RedWork w, cudaStream_t s);
-// w <- fma(-(*h), vi, w) and *res = dot(w, vnext) (or dot(w, w) if vnext is null)
-void launch_mgs(double* w, const double* vi, const double* h, const double* vnext, long long n,
-                double* res, RedWork rw, cudaStream_t s);
-// *hn = sqrt(*hsq), *ih = 1 / *hn; v = w * (*ih); *res = sum (v winv)^2
-void launch_scale_wsq(const double* w, const double* hsq, double* hn, double* ih, double* v,
-                      const double* winv, long long n, double* res, RedWork rw, cudaStream_t s);
-void launch_scale(const double* x, double a, double* y, long long n, cudaStream_t s);
-void launch_winv(const double* u, double rtol, double atol, double* winv, long long n, cudaStream_t s);
-// out = u + sum_i c[i] V_i
-void launch_combine(const double* u, const double* V, long long ldV, const double* c, int m,
-                    double* out, long long n, cudaStream_t s);
-// res = sum ((g1 - g0 - sum_i z_i V_i) * dt3 * winv)^2
+SegInfo single_segment(long long n, RedWork w);
+void launch_dot(const double* x, const double* y, const SegInfo& g, double* res, int rstride,
+                double* partials, cudaStream_t s);
+void launch_wsq(const double* x, const double* winv, const SegInfo& g, double* res, int rstride,
+                double* partials, cudaStream_t s);
+void launch_vsum(const double* x, const SegInfo& g, double* res, int rstride, double* partials,
+                 cudaStream_t s);
+// w <- fma(-h_s, vi, w), res_s = dot(w, vnext) (or dot(w, w) if vnext is null),
+// h_s = h[s * hstride]
+void launch_mgs(double* w, const double* vi, const double* h, int hstride, const double* vnext,
+                const SegInfo& g, double* res, int rstride, double* partials, cudaStream_t s);
+// hn_s = sqrt(hsq_s), ih_s = 1 / hn_s; v = w * ih_s; res_s = sum (v winv)^2
+// (hsq, hn, ih strided by `stride` per segment)
+void launch_scale_wsq(const double* w, const double* hsq, double* hn, double* ih, int stride,
+                      double* v, const double* winv, const SegInfo& g, double* res, double* partials,
+                      cudaStream_t s);
+// b = a and d = c on the active segments
+void launch_seg_copy2(const double* a, double* b, const double* c, double* d, const SegInfo& g,
+                      cudaStream_t s);
+// y = x * a_s (a strided)
+void launch_seg_scale(const double* x, const double* a, int astride, double* y, const SegInfo& g,
+                      cudaStream_t s);
+void launch_winv(const double* u, double rtol, double atol, double* winv, const SegInfo& g,
+                 cudaStream_t s);
+// out = u + sum_{q < m_s} c_s[q] V_q (c_s at c + s * cstride)
+void launch_combine(const double* u, const double* V, long long ldV, const double* c, int cstride,
+                    const int* m, double* out, const SegInfo& g, cudaStream_t s);
+// res_s = sum ((g1 - g0 - sum_{q < mz_s} z_s[q] V_q) * dt3_s * winv)^2
 void launch_err(const double* g1, const double* g0, const double* V, long long ldV, const double* z,
-                int mz, double dt3, const double* winv, long long n, double* res, RedWork rw,
-                cudaStream_t s);
+                int zstride, const int* mz, const double* dt3, int dstride, const double* winv,
+                const SegInfo& g, double* res, int rstride, double* partials, cudaStream_t s);
+
 // number of kernels this library has launched (host counter)
 unsigned long long kernel_launches();
 void add_launches(int n);
@@ -132,9 +169,9 @@ void set_counting(bool on);
 // measured FP64 instruction rate of the device (DFMA chains)
 int measure_fp64_peak(double* ops_per_s);
 
-// total water content
-void launch_water(const Problem& P, const double* u, double* terms, double* res, RedWork rw,
-                  cudaStream_t s);
+// water content terms, [macro nodes of s | cells of s] scenario by scenario
+// (reduce them with launch_vsum)
+void launch_water_terms(const Problem& P, const double* u, double* terms, cudaStream_t s);
 
 }  // namespace tsr
 

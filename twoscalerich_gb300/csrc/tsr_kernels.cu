@@ -187,6 +187,8 @@ __device__ __forceinline__ void macro_element_terms(const Problem& P, int k, con
 {
     const MacroDev& M = P.M;
     const int nv = M.nv, Ne = M.Ne;
+    // per-scenario factor on Keff (ensemble form)
+    const double ks = M.scen_kscale ? M.scen_kscale[k / M.scen_cells] : 1.0;
     double* out = P.contrib + (long long)16 * k;
     if (lane < nv) {
         const int j = lane;
@@ -196,6 +198,8 @@ __device__ __forceinline__ void macro_element_terms(const Problem& P, int k, con
         double Hf = interp_at(nv, al, mx, my);
         double K[4];
         keff_dev(Hf, M, T, K);
+        if (M.scen_kscale)
+            for (int q = 0; q < 4; ++q) K[q] *= ks;
         double gy1 = gy + 1.0;
         double qx = fma(K[0], gx, K[1] * gy1);
         double qy = fma(K[2], gx, K[3] * gy1);
@@ -217,6 +221,8 @@ __device__ __forceinline__ void macro_element_terms(const Problem& P, int k, con
             double Hb = interp_at(nv, al, bx, by);
             double K[4];
             keff_dev(Hb, M, T, K);
+            if (M.scen_kscale)
+                for (int q = 0; q < 4; ++q) K[q] *= ks;
             double gy1 = gy + 1.0;
             double qx = fma(K[0], gx, K[1] * gy1);
             double qy = fma(K[2], gx, K[3] * gy1);
@@ -249,10 +255,9 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
                                                 const double* __restrict__ epsv,
                                                 double* __restrict__ out)
 {
-    // finite-difference step and its reciprocal, from device memory so that
-    // a captured graph replays with the current values
-    const double eps = MODE ? epsv[0] : 0.0;
-    const double inv_eps = MODE ? epsv[1] : 0.0;
+    // The finite-difference step and its reciprocal come from device memory
+    // (one pair per scenario) so that a captured graph replays with the
+    // current values; cells of scenarios that are not active are skipped.
     extern __shared__ double sm[];
     tsr_math_tables* T = reinterpret_cast<tsr_math_tables*>(sm);
     double* misc = sm + kTabDoubles;                         // 16 per cell slot
@@ -266,10 +271,19 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
     const int nv = M.nv, Ne = M.Ne;
     const bool exch = (M.model_type == 3);
     load_tables(T);
-    int bad = 0;
+    int* cscen = ck + P.misc_slots;                          // scenario of each cell, -1 inactive
     for (int b = blockIdx.x; b < S.n_bundles; b += gridDim.x) {
-        __syncthreads();
         const int t = S.bundle_tpl[b], first = S.bundle_first[b], nc = S.bundle_count[b];
+        if (P.active) {
+            int any = 0;
+            for (int c = tid; c < nc; c += bs) {
+                const int k = S.bundle_cells[first + c];
+                any |= P.active[M.nscen > 1 ? k / M.scen_cells : 0];
+            }
+            if (!__syncthreads_or(any)) continue;
+        } else {
+            __syncthreads();
+        }
         const TplDesc D = S.tpl[t];
         const int mn = D.mn, mNe = D.mNe, nb = D.nb;
         double* h = st;
@@ -293,14 +307,24 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
         for (int c = warp; c < nc; c += nwarps) {
             const int k = S.bundle_cells[first + c];
             double* mc = misc + 16 * c;
+            const int sc = M.nscen > 1 ? k / M.scen_cells : 0;
+            const bool on = !P.active || P.active[sc];
+            const double eps = MODE ? epsv[(long long)sc * P.eps_stride] : 0.0;
             if (lane == 0) {
                 ck[c] = k;
+                cscen[c] = on ? sc : -1;
                 coff[c] = S.cell_off[k];
                 mc[4] = P.cell_scale ? P.cell_scale[k] : 1.0;
                 mc[5] = M.cent[k];
                 mc[6] = M.cent[Ne + k];
+                mc[12] = eps;
+                mc[13] = MODE ? epsv[(long long)sc * P.eps_stride + 1] : 0.0;
             }
-            if (lane < nv) mc[8 + lane] = state_at<MODE>(u, v, eps, M.elements[(long long)lane * Ne + k]);
+            if (lane < nv) {
+                long long vi = M.elements[(long long)lane * Ne + k];
+                if (M.node_off) vi = M.node_off[vi];
+                mc[8 + lane] = state_at<MODE>(u, v, eps, vi);
+            }
             __syncwarp();
             if (lane < nv) {
                 const int m = lane;
@@ -314,6 +338,7 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
         // nodes: head, conductivity, storage
         for (int idx = tid; idx < nc * mn; idx += bs) {
             const int c = idx / mn, l = idx - c * mn;
+            if (cscen[c] < 0) continue;
             const double* mc = misc + 16 * c;
             const double s = mc[4];
             const VGPar& pB = S.cell_par ? S.cell_par[ck[c]] : P.pB;
@@ -327,7 +352,7 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
                 }
                 hl = interp_at(nv, mc, px, py);
             } else {
-                hl = state_at<MODE>(u, v, eps, coff[c] + l);
+                hl = state_at<MODE>(u, v, mc[12], coff[c] + l);
             }
             h[idx] = hl;
             double K, Cn, Cdl;
@@ -340,6 +365,7 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
         // elements: SCV face fluxes and inclusion-boundary exchange items
         for (int idx = tid; idx < nc * mNe; idx += bs) {
             const int c = idx / mNe, e = idx - c * mNe;
+            if (cscen[c] < 0) continue;
             const double s = misc[16 * c + 4];
             const double* hc = h + c * mn;
             const double* Khc = Kh + c * mn;
@@ -376,6 +402,7 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
         // nodes: gather face fluxes in the fixed order, divide by storage
         for (int idx = tid; idx < nc * mn; idx += bs) {
             const int c = idx / mn, l = idx - c * mn;
+            if (cscen[c] < 0) continue;
             double g;
             if (bnode[l]) {
                 g = 0.0;
@@ -390,15 +417,16 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
                 }
                 g = (acc * Cd[idx]) / den[idx];
             }
-            if (!finite_d(g)) bad = 1;
+            if (!finite_d(g)) atomicOr(P.flag + cscen[c], 1);
             const long long o = coff[c] + l;
             if (MODE == 0)
                 out[o] = g;
             else
-                out[o] = (g - g0[o]) * inv_eps;
+                out[o] = (g - g0[o]) * misc[16 * c + 13];
         }
         // exchange flux and the macro element terms: one warp per cell
         for (int c = warp; c < nc; c += nwarps) {
+            if (cscen[c] < 0) continue;
             double Q = 0.0;
             if (exch) {
                 const double* it = items + c * nb;
@@ -411,7 +439,6 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
             macro_element_terms(P, ck[c], misc + 16 * c, Q, T, lane);
         }
     }
-    if (bad) atomicOr(P.flag, 1);
 }
 
 // ---- macro nodes ----------------------------------------------------------
@@ -422,19 +449,21 @@ __global__ void __launch_bounds__(128) k_macro_nodes(Problem P, const double* __
                                                      const double* __restrict__ epsv,
                                                      double* __restrict__ out)
 {
-    const double eps = MODE ? epsv[0] : 0.0;
-    const double inv_eps = MODE ? epsv[1] : 0.0;
     __shared__ tsr_math_tables T;
     load_tables(&T);
     __syncthreads();
     const MacroDev& M = P.M;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= M.Mn) return;
+    const int sc = M.nscen > 1 ? i / M.scen_nodes : 0;
+    if (P.active && !P.active[sc]) return;
+    const long long o = M.node_off ? M.node_off[i] : i;
     double g;
     if (M.dirichlet[i]) {
         g = 0.0;
     } else {
-        const double H = state_at<MODE>(u, v, eps, i);
+        const double eps = MODE ? epsv[(long long)sc * P.eps_stride] : 0.0;
+        const double H = state_at<MODE>(u, v, eps, o);
         double acc = 0.0;
         const int p1 = M.csr_ptr[i + 1];
         for (int p = M.csr_ptr[i]; p < p1; ++p) {
@@ -443,16 +472,16 @@ __global__ void __launch_bounds__(128) k_macro_nodes(Problem P, const double* __
             acc = (ent & 1) ? (acc - c) : (acc + c);
         }
         double Cn, Cd;
-        vg_storage(H, P.pA, &T, Cn, Cd);
+        vg_storage(H, M.scen_pA ? M.scen_pA[sc] : P.pA, &T, Cn, Cd);
         const double A = M.epsA * M.cv[i];
         const double den = fma(M.Ss, Cd, Cn) * A;
         g = (acc * Cd) / den;
     }
-    if (!finite_d(g)) atomicOr(P.flag, 1);
+    if (!finite_d(g)) atomicOr(P.flag + sc, 1);
     if (MODE == 0)
-        out[i] = g;
+        out[o] = g;
     else
-        out[i] = (g - g0[i]) * inv_eps;
+        out[o] = (g - g0[o]) * epsv[(long long)sc * P.eps_stride + 1];
 }
 
 int configure_cell_kernels(const Problem& P, int* occ)
@@ -487,14 +516,61 @@ void launch_g(const Problem& P, int mode, const double* u, const double* v, cons
 }
 
 // ---- fixed-order reductions ------------------------------------------------
-// Block b covers items [8192 b, 8192 (b+1)); thread t sums items
-// 8192 b + 256 s + t (s ascending); warps combine by xor butterfly, the 8
-// warp sums as ((w0+w1)+(w2+w3))+((w4+w5)+(w6+w7)).  The last block to
-// finish reduces the block sums the same way (thread t: P[t], P[t+256], ...).
+// Within a segment (a whole vector, or one scenario's part of it), block b
+// covers items [8192 b, 8192 (b+1)) relative to the segment's start; thread t
+// sums items 8192 b + 256 s + t (s ascending); warps combine by xor
+// butterfly, the 8 warp sums as ((w0+w1)+(w2+w3))+((w4+w5)+(w6+w7)).  The
+// last block of the segment to finish reduces its block sums the same way
+// (thread t: P[t], P[t+256], ...).  A segment is therefore reduced exactly
+// as it would be on its own.
 static constexpr int kRedThreads = 256;
 static constexpr int kRedChunk = 8192;
 
-int reduction_blocks(long long n) { return (int)((n + kRedChunk - 1) / kRedChunk); }
+int reduction_blocks(long long n)
+{
+    long long b = (n + kRedChunk - 1) / kRedChunk;
+    return (int)(b > 0 ? b : 1);
+}
+
+SegInfo single_segment(long long n, RedWork w)
+{
+    SegInfo g{};
+    g.nseg = 1;
+    g.nblocks = reduction_blocks(n);
+    g.n1 = n;
+    g.counters = w.counter;
+    return g;
+}
+
+struct SegBlock {
+    int s;          // segment
+    long long lo;   // first item of the segment
+    long long hi;   // one past its last item
+    int lb;         // block index within the segment
+    int b0;         // first block of the segment
+    int nb;         // blocks of the segment
+};
+
+__device__ __forceinline__ SegBlock seg_block(const SegInfo& g)
+{
+    SegBlock r;
+    if (g.start) {
+        r.s = g.blkseg[blockIdx.x];
+        r.lo = g.start[r.s];
+        r.hi = g.start[r.s + 1];
+        r.b0 = g.block0[r.s];
+        r.nb = g.block0[r.s + 1] - r.b0;
+        r.lb = (int)blockIdx.x - r.b0;
+    } else {
+        r.s = 0;
+        r.lo = 0;
+        r.hi = g.n1;
+        r.b0 = 0;
+        r.nb = (int)gridDim.x;
+        r.lb = (int)blockIdx.x;
+    }
+    return r;
+}
 
 __device__ __forceinline__ double block_sum_256(double a, double* ws)
 {
@@ -510,8 +586,8 @@ __device__ __forceinline__ double block_sum_256(double a, double* ws)
 }
 
 // called by all threads with the block's partial sum (valid on thread 0)
-__device__ __forceinline__ void finish_reduction(double r, double* partials, unsigned int* counter,
-                                                 double* res)
+__device__ __forceinline__ void finish_reduction(double r, const SegBlock& B, double* partials,
+                                                 unsigned int* counter, double* res)
 {
     __shared__ double ws[8];
     __shared__ int last;
@@ -519,13 +595,13 @@ __device__ __forceinline__ void finish_reduction(double r, double* partials, uns
         partials[blockIdx.x] = r;
         __threadfence();
         unsigned int prev = atomicAdd(counter, 1u);
-        last = (prev == gridDim.x - 1);
+        last = (prev == (unsigned int)(B.nb - 1));
     }
     __syncthreads();
     if (!last) return;
     __threadfence();
     double a = 0.0;
-    for (int i = threadIdx.x; i < (int)gridDim.x; i += kRedThreads) a = a + __ldcg(partials + i);
+    for (int i = threadIdx.x; i < B.nb; i += kRedThreads) a = a + __ldcg(partials + B.b0 + i);
     double tot = block_sum_256(a, ws);
     if (threadIdx.x == 0) {
         *res = tot;
@@ -534,34 +610,36 @@ __device__ __forceinline__ void finish_reduction(double r, double* partials, uns
 }
 
 template <class Term>
-__global__ void __launch_bounds__(kRedThreads) k_reduce(Term term, long long n, double* partials,
-                                                        unsigned int* counter, double* res)
+__global__ void __launch_bounds__(kRedThreads) k_reduce(Term term, SegInfo g, double* partials,
+                                                        double* res, int rstride)
 {
     __shared__ double ws[8];
-    const long long base = (long long)blockIdx.x * kRedChunk + threadIdx.x;
+    const SegBlock B = seg_block(g);
+    if (g.active && !g.active[B.s]) return;
+    const long long base = B.lo + (long long)B.lb * kRedChunk + threadIdx.x;
     double a = 0.0;
 #pragma unroll 4
-    for (int s = 0; s < kRedChunk / kRedThreads; ++s) {
-        const long long i = base + (long long)s * kRedThreads;
-        if (i < n) a = term(i, a);
+    for (int q = 0; q < kRedChunk / kRedThreads; ++q) {
+        const long long i = base + (long long)q * kRedThreads;
+        if (i < B.hi) a = term(B.s, i, a);
     }
     double r = block_sum_256(a, ws);
-    finish_reduction(r, partials, counter, res);
+    finish_reduction(r, B, partials, g.counters + B.s, res + (long long)B.s * rstride);
 }
 
 struct TermDot {
     const double* x;
     const double* y;
-    __device__ double operator()(long long i, double a) const { return fma(x[i], y[i], a); }
+    __device__ double operator()(int, long long i, double a) const { return fma(x[i], y[i], a); }
 };
 struct TermSum {
     const double* x;
-    __device__ double operator()(long long i, double a) const { return a + x[i]; }
+    __device__ double operator()(int, long long i, double a) const { return a + x[i]; }
 };
 struct TermWsq {
     const double* x;
     const double* w;
-    __device__ double operator()(long long i, double a) const
+    __device__ double operator()(int, long long i, double a) const
     {
         double r = x[i] * w[i];
         return fma(r, r, a);
@@ -571,10 +649,11 @@ struct TermMgs {
     double* w;
     const double* vi;
     const double* h;
+    int hstride;
     const double* vn;
-    __device__ double operator()(long long i, double a) const
+    __device__ double operator()(int s, long long i, double a) const
     {
-        double wn = fma(-(*h), vi[i], w[i]);
+        double wn = fma(-h[(long long)s * hstride], vi[i], w[i]);
         w[i] = wn;
         return fma(wn, vn ? vn[i] : wn, a);
     }
@@ -582,11 +661,12 @@ struct TermMgs {
 struct TermScaleWsq {
     const double* w;
     const double* ih;
+    int stride;
     double* v;
     const double* winv;
-    __device__ double operator()(long long i, double a) const
+    __device__ double operator()(int s, long long i, double a) const
     {
-        double vv = w[i] * (*ih);
+        double vv = w[i] * ih[(long long)s * stride];
         v[i] = vv;
         double r = vv * winv[i];
         return fma(r, r, a);
@@ -598,123 +678,185 @@ struct TermErr {
     const double* V;
     long long ldV;
     const double* z;
-    int mz;
-    double dt3;
+    int zstride;
+    const int* mz;
+    const double* dt3;
+    int dstride;
     const double* winv;
-    __device__ double operator()(long long i, double a) const
+    __device__ double operator()(int s, long long i, double a) const
     {
+        const double* zs = z + (long long)s * zstride;
+        const int m = mz[s];
         double d = g1[i] - g0[i];
-        for (int q = 0; q < mz; ++q) d = fma(-z[q], V[(long long)q * ldV + i], d);
-        double e = d * dt3;
+        for (int q = 0; q < m; ++q) d = fma(-zs[q], V[(long long)q * ldV + i], d);
+        double e = d * dt3[(long long)s * dstride];
         double r = e * winv[i];
         return fma(r, r, a);
     }
 };
 
-void launch_dot(const double* x, const double* y, long long n, double* res, RedWork w, cudaStream_t s)
+template <class Term>
+static void run_reduce(const Term& t, const SegInfo& g, double* res, int rstride, double* partials,
+                       cudaStream_t s)
 {
     count();
-    k_reduce<<<reduction_blocks(n), kRedThreads, 0, s>>>(TermDot{x, y}, n, w.partials, w.counter, res);
-}
-void launch_vsum(const double* x, long long n, double* res, RedWork w, cudaStream_t s)
-{
-    count();
-    k_reduce<<<reduction_blocks(n), kRedThreads, 0, s>>>(TermSum{x}, n, w.partials, w.counter, res);
-}
-void launch_wsq(const double* x, const double* winv, long long n, double* res, RedWork w, cudaStream_t s)
-{
-    count();
-    k_reduce<<<reduction_blocks(n), kRedThreads, 0, s>>>(TermWsq{x, winv}, n, w.partials, w.counter, res);
-}
-void launch_mgs(double* w, const double* vi, const double* h, const double* vnext, long long n,
-                double* res, RedWork rw, cudaStream_t s)
-{
-    count();
-    k_reduce<<<reduction_blocks(n), kRedThreads, 0, s>>>(TermMgs{w, vi, h, vnext}, n, rw.partials,
-                                                         rw.counter, res);
+    k_reduce<<<g.nblocks, kRedThreads, 0, s>>>(t, g, partials, res, rstride);
 }
 
-// h = sqrt(hsq) (stored as H(j+1,j)) and its reciprocal, once
-__global__ void k_store_sqrt(const double* hsq, double* hn, double* ih)
+void launch_dot(const double* x, const double* y, const SegInfo& g, double* res, int rstride,
+                double* partials, cudaStream_t s)
 {
-    double h = sqrt(*hsq);
-    *hn = h;
-    *ih = 1.0 / h;
+    run_reduce(TermDot{x, y}, g, res, rstride, partials, s);
+}
+void launch_vsum(const double* x, const SegInfo& g, double* res, int rstride, double* partials,
+                 cudaStream_t s)
+{
+    run_reduce(TermSum{x}, g, res, rstride, partials, s);
+}
+void launch_wsq(const double* x, const double* winv, const SegInfo& g, double* res, int rstride,
+                double* partials, cudaStream_t s)
+{
+    run_reduce(TermWsq{x, winv}, g, res, rstride, partials, s);
+}
+void launch_mgs(double* w, const double* vi, const double* h, int hstride, const double* vnext,
+                const SegInfo& g, double* res, int rstride, double* partials, cudaStream_t s)
+{
+    run_reduce(TermMgs{w, vi, h, hstride, vnext}, g, res, rstride, partials, s);
 }
 
-void launch_scale_wsq(const double* w, const double* hsq, double* hn, double* ih, double* v,
-                      const double* winv, long long n, double* res, RedWork rw, cudaStream_t s)
+// per segment: h = sqrt(hsq) (stored as H(j+1,j)) and its reciprocal, once
+__global__ void k_store_sqrt(const double* hsq, double* hn, double* ih, int stride, int nseg,
+                             const int* active)
 {
-    count(2);
-    k_store_sqrt<<<1, 1, 0, s>>>(hsq, hn, ih);
-    k_reduce<<<reduction_blocks(n), kRedThreads, 0, s>>>(TermScaleWsq{w, ih, v, winv}, n, rw.partials,
-                                                         rw.counter, res);
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nseg || (active && !active[s])) return;
+    const long long o = (long long)s * stride;
+    double h = sqrt(hsq[o]);
+    hn[o] = h;
+    ih[o] = 1.0 / h;
 }
+
+void launch_scale_wsq(const double* w, const double* hsq, double* hn, double* ih, int stride,
+                      double* v, const double* winv, const SegInfo& g, double* res, double* partials,
+                      cudaStream_t s)
+{
+    count();
+    k_store_sqrt<<<(g.nseg + 127) / 128, 128, 0, s>>>(hsq, hn, ih, stride, g.nseg, g.active);
+    run_reduce(TermScaleWsq{w, ih, stride, v, winv}, g, res, stride, partials, s);
+}
+
 void launch_err(const double* g1, const double* g0, const double* V, long long ldV, const double* z,
-                int mz, double dt3, const double* winv, long long n, double* res, RedWork rw,
-                cudaStream_t s)
+                int zstride, const int* mz, const double* dt3, int dstride, const double* winv,
+                const SegInfo& g, double* res, int rstride, double* partials, cudaStream_t s)
 {
-    count();
-    k_reduce<<<reduction_blocks(n), kRedThreads, 0, s>>>(TermErr{g1, g0, V, ldV, z, mz, dt3, winv}, n,
-                                                         rw.partials, rw.counter, res);
+    run_reduce(TermErr{g1, g0, V, ldV, z, zstride, mz, dt3, dstride, winv}, g, res, rstride, partials, s);
 }
 
-// ---- elementwise -------------------------------------------------------------
-__global__ void k_scale(const double* __restrict__ x, double a, double* __restrict__ y, long long n)
+// ---- elementwise, over segments (same block mapping as the reductions) -------
+template <class Op>
+__global__ void __launch_bounds__(kRedThreads) k_segmap(Op op, SegInfo g)
 {
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x)
-        y[i] = x[i] * a;
-}
-__global__ void k_winv(const double* __restrict__ u, double rtol, double atol, double* __restrict__ w,
-                       long long n)
-{
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x)
-        w[i] = 1.0 / fma(rtol, fabs(u[i]), atol);
-}
-__global__ void k_combine(const double* __restrict__ u, const double* __restrict__ V, long long ldV,
-                          const double* __restrict__ c, int m, double* __restrict__ out, long long n)
-{
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x) {
-        double a = u[i];
-        for (int q = 0; q < m; ++q) a = fma(c[q], V[(long long)q * ldV + i], a);
-        out[i] = a;
+    const SegBlock B = seg_block(g);
+    if (g.active && !g.active[B.s]) return;
+    const long long base = B.lo + (long long)B.lb * kRedChunk + threadIdx.x;
+#pragma unroll 4
+    for (int q = 0; q < kRedChunk / kRedThreads; ++q) {
+        const long long i = base + (long long)q * kRedThreads;
+        if (i < B.hi) op(B.s, i);
     }
 }
 
-static int ew_grid(long long n)
-{
-    long long b = (n + 255) / 256;
-    return (int)(b < 152LL * 32 ? (b > 0 ? b : 1) : 152LL * 32);
-}
+struct OpScale {
+    const double* x;
+    const double* a;
+    int astride;
+    double* y;
+    __device__ void operator()(int s, long long i) const { y[i] = x[i] * a[(long long)s * astride]; }
+};
+struct OpWinv {
+    const double* u;
+    double rtol, atol;
+    double* w;
+    __device__ void operator()(int, long long i) const { w[i] = 1.0 / fma(rtol, fabs(u[i]), atol); }
+};
+struct OpCombine {
+    const double* u;
+    const double* V;
+    long long ldV;
+    const double* c;
+    int cstride;
+    const int* m;
+    double* out;
+    __device__ void operator()(int s, long long i) const
+    {
+        const double* cs = c + (long long)s * cstride;
+        const int ms = m[s];
+        double a = u[i];
+        for (int q = 0; q < ms; ++q) a = fma(cs[q], V[(long long)q * ldV + i], a);
+        out[i] = a;
+    }
+};
 
-void launch_scale(const double* x, double a, double* y, long long n, cudaStream_t s)
+struct OpCopy2 {
+    const double* a;
+    double* b;
+    const double* c;
+    double* d;
+    __device__ void operator()(int, long long i) const
+    {
+        b[i] = a[i];
+        d[i] = c[i];
+    }
+};
+
+void launch_seg_copy2(const double* a, double* b, const double* c, double* d, const SegInfo& g,
+                      cudaStream_t s)
 {
     count();
-    k_scale<<<ew_grid(n), 256, 0, s>>>(x, a, y, n);
+    k_segmap<<<g.nblocks, kRedThreads, 0, s>>>(OpCopy2{a, b, c, d}, g);
 }
-void launch_winv(const double* u, double rtol, double atol, double* winv, long long n, cudaStream_t s)
+void launch_seg_scale(const double* x, const double* a, int astride, double* y, const SegInfo& g,
+                      cudaStream_t s)
 {
     count();
-    k_winv<<<ew_grid(n), 256, 0, s>>>(u, rtol, atol, winv, n);
+    k_segmap<<<g.nblocks, kRedThreads, 0, s>>>(OpScale{x, a, astride, y}, g);
 }
-void launch_combine(const double* u, const double* V, long long ldV, const double* c, int m,
-                    double* out, long long n, cudaStream_t s)
+void launch_winv(const double* u, double rtol, double atol, double* winv, const SegInfo& g,
+                 cudaStream_t s)
 {
     count();
-    k_combine<<<ew_grid(n), 256, 0, s>>>(u, V, ldV, c, m, out, n);
+    k_segmap<<<g.nblocks, kRedThreads, 0, s>>>(OpWinv{u, rtol, atol, winv}, g);
+}
+void launch_combine(const double* u, const double* V, long long ldV, const double* c, int cstride,
+                    const int* m, double* out, const SegInfo& g, cudaStream_t s)
+{
+    count();
+    k_segmap<<<g.nblocks, kRedThreads, 0, s>>>(OpCombine{u, V, ldV, c, cstride, m, out}, g);
 }
 
 // ---- total water content --------------------------------------------------
+// Terms are laid out scenario by scenario: [macro nodes of s | cells of s].
+__device__ __forceinline__ long long water_slot_node(const MacroDev& M, int i)
+{
+    if (M.nscen <= 1) return i;
+    const int s = i / M.scen_nodes;
+    return (long long)s * (M.scen_nodes + M.scen_cells) + (i - s * M.scen_nodes);
+}
+__device__ __forceinline__ long long water_slot_cell(const MacroDev& M, int k)
+{
+    if (M.nscen <= 1) return (long long)M.Mn + k;
+    const int s = k / M.scen_cells;
+    return (long long)s * (M.scen_nodes + M.scen_cells) + M.scen_nodes + (k - s * M.scen_cells);
+}
+
 __global__ void k_water_macro(Problem P, const double* __restrict__ u, double* __restrict__ terms)
 {
     const MacroDev& M = P.M;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= M.Mn) return;
-    double Se = vg_se(u[i], P.pA, &d_tables);
-    terms[i] = (M.epsA * M.cv[i]) * fma(P.pA.dth, Se, P.pA.thr);
+    const VGPar& pA = M.scen_pA ? M.scen_pA[i / M.scen_nodes] : P.pA;
+    double Se = vg_se(u[M.node_off ? M.node_off[i] : i], pA, &d_tables);
+    terms[water_slot_node(M, i)] = (M.epsA * M.cv[i]) * fma(pA.dth, Se, pA.thr);
 }
 
 // one warp per cell; lane l sums nodes l, l+32, ... (the fixed lane order)
@@ -734,9 +876,14 @@ __global__ void k_water_cells(Problem P, const double* __restrict__ u, double* _
     const VGPar& pB = S.cell_par ? S.cell_par[k] : P.pB;
     double al[4];
     for (int m = 0; m < nv; ++m) {
-        double a = M.sf[(long long)(m * nv) * Ne + k] * u[M.elements[k]];
-        for (int i = 1; i < nv; ++i)
-            a = fma(M.sf[(long long)(m * nv + i) * Ne + k], u[M.elements[(long long)i * Ne + k]], a);
+        long long v0 = M.elements[k];
+        if (M.node_off) v0 = M.node_off[v0];
+        double a = M.sf[(long long)(m * nv) * Ne + k] * u[v0];
+        for (int i = 1; i < nv; ++i) {
+            long long vi = M.elements[(long long)i * Ne + k];
+            if (M.node_off) vi = M.node_off[vi];
+            a = fma(M.sf[(long long)(m * nv + i) * Ne + k], u[vi], a);
+        }
         al[m] = a;
     }
     const double s = P.cell_scale ? P.cell_scale[k] : 1.0;
@@ -763,17 +910,15 @@ __global__ void k_water_cells(Problem P, const double* __restrict__ u, double* _
     if (lane == 0) {
         double area = M.scv[k];
         for (int j = 1; j < nv; ++j) area += M.scv[(long long)j * Ne + k];
-        terms[M.Mn + k] = (area * M.inv_Y) * ((s * s) * p);
+        terms[water_slot_cell(M, k)] = (area * M.inv_Y) * ((s * s) * p);
     }
 }
 
-void launch_water(const Problem& P, const double* u, double* terms, double* res, RedWork rw,
-                  cudaStream_t s)
+void launch_water_terms(const Problem& P, const double* u, double* terms, cudaStream_t s)
 {
     count(2);
     k_water_macro<<<(P.M.Mn + 127) / 128, 128, 0, s>>>(P, u, terms);
     k_water_cells<<<(P.M.Ne * 32 + 127) / 128, 128, 0, s>>>(P, u, terms);
-    launch_vsum(terms, (long long)P.M.Mn + P.M.Ne, res, rw, s);
 }
 
 }  // namespace tsr

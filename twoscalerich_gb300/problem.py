@@ -54,7 +54,8 @@ class Problem:
     def __init__(self, macro, micro, keff_rows, epsA, soilA, soilB, *, macro_bc,
                  model_type=3, boundary_flux=0.0, dirichlet_h=0.0, specific_storage=1e-6,
                  kface=0, cell_scale=None, logh_first=None, logr=None, name="",
-                 templates=None, cell_template=None, cell_soilB=None):
+                 templates=None, cell_template=None, cell_soilB=None, scenarios=1,
+                 scen_soilA=None, scen_keff_scale=None):
         """micro: the micro mesh of every cell; or, for the batched form,
         templates (list of micro meshes) with cell_template[k] naming the
         template of cell k and optional per-cell material B (list of dicts)."""
@@ -127,6 +128,33 @@ class Problem:
             self.cell_nodes = np.full(self.Ne, self.mn, dtype=np.int64)
             self.cell_off = self.Mn + self.mn * np.arange(self.Ne, dtype=np.int64)
             self.N = self.Mn + self.Ne * self.mn
+        if templates is None and cell_soilB is not None:
+            self._soils = (capi.Soil * self.Ne)(*[make_soil(**s) for s in cell_soilB])
+            self.ext.cell_soilB = C.cast(self._soils, C.POINTER(capi.Soil))
+        # scenario-major layout of the unknowns: [macro_s | cells_s] per scenario
+        self.S = scenarios
+        Mn_s, Ne_s = self.Mn // scenarios, self.Ne // scenarios
+        self.node_off = np.empty(self.Mn, dtype=np.int64)
+        self.scen_start = np.zeros(scenarios + 1, dtype=np.int64)
+        off = 0
+        cell_off = np.empty(self.Ne, dtype=np.int64)
+        for s in range(scenarios):
+            self.scen_start[s] = off
+            self.node_off[s * Mn_s:(s + 1) * Mn_s] = off + np.arange(Mn_s)
+            off += Mn_s
+            cn = self.cell_nodes[s * Ne_s:(s + 1) * Ne_s]
+            cell_off[s * Ne_s:(s + 1) * Ne_s] = off + np.concatenate([[0], np.cumsum(cn)[:-1]])
+            off += int(cn.sum())
+        self.scen_start[scenarios] = off
+        self.cell_off = cell_off
+        if scenarios > 1:
+            self.ext.scenarios = scenarios
+            if scen_soilA is not None:
+                self._scenA = (capi.Soil * scenarios)(*[make_soil(**s) for s in scen_soilA])
+                self.ext.scen_soilA = C.cast(self._scenA, C.POINTER(capi.Soil))
+            if scen_keff_scale is not None:
+                self._kscale = np.ascontiguousarray(scen_keff_scale, dtype=np.float64)
+                self.ext.scen_keff_scale = ptr(self._kscale)
         self.ud.N = self.N
         self.dirichlet_h = dirichlet_h
         bce = capi.as_array(self.macro.boundary_condition_edges, macro.nv * self.Ne, np.int32)
@@ -143,11 +171,20 @@ class Problem:
         self.tend = 1.0
 
     def initial_state(self, h0=-5.0, noise=0.0, seed=EVAL_SEED):
-        u = np.full(self.N, h0, dtype=np.float64)
+        """h0 (a number, or one number per scenario) plus optional noise;
+        Dirichlet nodes at their head."""
+        h0 = np.broadcast_to(np.asarray(h0, dtype=np.float64), (self.S,))
+        u = np.empty(self.N, dtype=np.float64)
+        for s in range(self.S):
+            u[self.scen_start[s]:self.scen_start[s + 1]] = h0[s]
         if noise > 0.0:
             u += np.random.default_rng(seed).normal(0.0, noise, self.N)
-        u[:self.Mn][self.dirichlet_nodes] = self.dirichlet_h
+        u[self.node_off[self.dirichlet_nodes]] = self.dirichlet_h
         return u
+
+    def scenario(self, u, s):
+        """The unknowns of scenario s (a view)."""
+        return u[self.scen_start[s]:self.scen_start[s + 1]]
 
     def array(self, name, n, dtype=np.float64, micro=False):
         s = self.micro if micro else self.macro
@@ -257,6 +294,72 @@ def config3(n_macro=151, seed=GENERATOR_SEED, eval_seed=EVAL_SEED):
     return p
 
 
+def union_mesh(mesh, copies):
+    """`copies` disjoint copies of a macro mesh, block s numbered after s-1."""
+    n, nv = mesh.n_nodes, mesh.nv
+    xy = np.concatenate([np.tile(mesh.xy[:n], copies), np.tile(mesh.xy[n:], copies)])
+    el = np.concatenate([mesh.elems + s * n for s in range(copies)])
+    b = mesh.bedges.reshape(-1, 3)
+    bed = np.concatenate([np.column_stack([b[:, 0] + s * n, b[:, 1] + s * n, b[:, 2]])
+                          for s in range(copies)])
+    return meshgen.Mesh(nv, xy, el, bed.ravel())
+
+
+def config4(scenarios=64, n_macro=51, n_micro=15, seed=GENERATOR_SEED, eval_seed=EVAL_SEED):
+    """Ensemble: `scenarios` independent problems solved together, each on an
+    n_macro^2 macro grid with n_micro^2 micro meshes (square inclusion of
+    side 0.5), Dirichlet top h = -0.1, no flow elsewhere.  Per scenario:
+    Ks_A ~ LogNormal(ln 0.054, 0.5), Ks_B ~ LogNormal(ln 0.001, 0.5),
+    alpha_A ~ U(1.5, 4.0), n_A ~ U(1.8, 2.6), Keff scaled by Ks_A / 0.054,
+    initial head U(-10, -1) m.  EXPREM tol 1e-6, Krylov <= 30, t_end = 1 d,
+    each scenario with its own step size and Krylov dimension."""
+    h = 1.0 / (n_macro - 1)
+    base = meshgen.macro_unit_square(n_macro)
+    macro = union_mesh(base, scenarios)
+    micro = meshgen.micro_square_inclusion(n_micro, cell=h, side=0.5)
+    rng = np.random.default_rng(seed)
+    ksA = rng.lognormal(np.log(0.054), 0.5, scenarios)
+    ksB = rng.lognormal(np.log(0.001), 0.5, scenarios)
+    alA = rng.uniform(1.5, 4.0, scenarios)
+    nA = rng.uniform(1.8, 2.6, scenarios)
+    h0 = np.random.default_rng(eval_seed).uniform(-10.0, -1.0, scenarios)
+    soilsA = [dict(SOIL_A, Ksat=k, alpha=a, n=n) for k, a, n in zip(ksA, alA, nA)]
+    soilsB = [dict(SOIL_B, Ksat=k) for k in ksB]
+    Ne_s = 2 * (n_macro - 1) ** 2
+    cellB = [soilsB[s] for s in range(scenarios) for _ in range(Ne_s)]
+    p = Problem(macro, micro, constant_keff_rows(0.02), 0.75, SOIL_A, SOIL_B,
+                macro_bc=[5, 2, 2, 2, 2], model_type=3, dirichlet_h=-0.1, cell_soilB=cellB,
+                scenarios=scenarios, scen_soilA=soilsA, scen_keff_scale=ksA / 0.054,
+                name="config4_%dx%d_%d" % (scenarios, n_macro, n_micro))
+    p.options = default_options(AbsTol=1e-6, RelTol=1e-6, MaxKrylov=30)
+    p.tend = 1.0
+    p.tspan = np.array([0.0])
+    p.h0 = h0
+    p.u0 = p.initial_state(h0)
+    p.scenario_params = dict(Ks_A=ksA, Ks_B=ksB, alpha_A=alA, n_A=nA, h0=h0)
+    return p
+
+
+def scenario_problem(ens, s):
+    """Scenario s of an ensemble as a standalone problem (same unknowns)."""
+    pr = ens.scenario_params
+    n_macro = int(round(np.sqrt(ens.Mn // ens.S)))
+    h = 1.0 / (n_macro - 1)
+    n_micro = int(round(np.sqrt(ens.mn)))
+    macro = meshgen.macro_unit_square(n_macro)
+    micro = meshgen.micro_square_inclusion(n_micro, cell=h, side=0.5)
+    K = constant_keff_rows(0.02 * (pr["Ks_A"][s] / 0.054))    # the ensemble's scale, same rounding
+    p = Problem(macro, micro, K, 0.75, dict(SOIL_A, Ksat=pr["Ks_A"][s], alpha=pr["alpha_A"][s],
+                                            n=pr["n_A"][s]),
+                dict(SOIL_B, Ksat=pr["Ks_B"][s]), macro_bc=[5, 2, 2, 2, 2], model_type=3,
+                dirichlet_h=-0.1, name="scenario%d" % s)
+    p.options = ens.options
+    p.tend = ens.tend
+    p.tspan = np.array([0.0])
+    p.u0 = np.ascontiguousarray(ens.scenario(ens.u0, s))
+    return p
+
+
 def fixture10(boundary_flux=0.05, jitter=0.25, seed=GENERATOR_SEED):
     """The shape of the reference's test scenario: 10x10 quadrilaterals,
     influx segment x in [0, 0.4] on the top (BC 1), free drainage dh/dx = 0
@@ -323,6 +426,37 @@ class Context:
         check(self.lib.tsr_exprem_step(self.h, C.byref(tt), self.p.tend, ptr(tspan), ptr(solns),
                                        ptr(u), C.byref(opts), C.byref(stats)), "tsr_exprem_step")
         return tt.value
+
+    # ---- ensembles: all scenarios of the context in lockstep
+    def load(self, u, t=0.0):
+        check(self.lib.tsr_exprem_load(self.h, ptr(u), t), "tsr_exprem_load")
+
+    def store(self):
+        u = np.empty(self.N)
+        check(self.lib.tsr_exprem_store(self.h, ptr(u)), "tsr_exprem_store")
+        return u
+
+    def ensemble_advance(self, stats, tspan=None, solns=None):
+        """One accepted step of every scenario short of tend.  stats: a
+        ctypes array of S ExpremStats (kept between calls).  Returns
+        (t per scenario, status per scenario, number still running)."""
+        S = self.p.S
+        tspan = np.array([0.0]) if tspan is None else np.ascontiguousarray(tspan, dtype=np.float64)
+        t = np.empty(S)
+        status = (C.c_int * S)()
+        nrun = C.c_int()
+        rows = None
+        if solns is not None:
+            rows = (capi.dp * S)(*[ptr(a) if a is not None else None for a in solns])
+        check(self.lib.tsr_ensemble_advance(self.h, self.p.tend, ptr(tspan), rows, C.byref(self.p.options),
+                                            stats, ptr(t), status, C.byref(nrun)),
+              "tsr_ensemble_advance")
+        return t, np.array(status[:]), nrun.value
+
+    def ensemble_water(self, u):
+        w = np.empty(self.p.S)
+        check(self.lib.tsr_ensemble_water(self.h, ptr(u), ptr(w)), "tsr_ensemble_water")
+        return w
 
     def close(self):
         if self.h:
