@@ -202,6 +202,63 @@ void tsr_release_all(void);
 int tsr_autotune(tsr_ctx* ctx, const double* u_host, int reps, double* best_ms,
                  int* best_threads, int* best_budget);
 
+/* ---- learned closure network (no reference counterpart) ----------------
+ * The closure's MLP: 6 inputs -> 4 hidden layers of 64 (SiLU) -> 2 outputs,
+ * BF16 weights and activations with FP32 accumulation on the tensor cores.
+ * Parameters are a flat FP32 block of tsr_mlp_num_params() floats:
+ * W1 [64 x 16] (input columns 6..15 zero), b1 [64], W2..W4 [64 x 64],
+ * b2..b4 [64], W5 [8 x 64] (rows 2..7 zero), b5 [8]; W row-major [out][in].
+ * Inputs are rows of 8 floats (6 used), outputs rows of 2 floats. */
+typedef struct tsr_mlp tsr_mlp;
+int      tsr_mlp_num_params(void);
+tsr_mlp* tsr_mlp_create(void);
+void     tsr_mlp_free(tsr_mlp* mlp);
+int      tsr_mlp_set_params(tsr_mlp* mlp, const float* params);
+int      tsr_mlp_get_params(tsr_mlp* mlp, float* params);
+/* y = MLP(x) for n rows (host arrays); fused = 1: the fused inference kernel
+ * (activations in registers), 0: the layer-by-layer training path */
+int      tsr_mlp_forward(tsr_mlp* mlp, const float* x, int n, float* y, int fused);
+/* mean squared error of n rows and its gradient (tsr_mlp_num_params floats) */
+int      tsr_mlp_grad(tsr_mlp* mlp, const float* x, const float* y, int n, float* loss,
+                      float* grad);
+/* training set (n rows, copied to the device) and minibatch AdamW training:
+ * `epochs` passes in a seeded random order, cosine-decayed learning rate */
+int      tsr_mlp_set_data(tsr_mlp* mlp, const float* x, const float* y, long long n);
+int      tsr_mlp_train(tsr_mlp* mlp, int epochs, int batch, float lr, float weight_decay,
+                       unsigned long long seed, float* loss_per_epoch);
+/* one AdamW step with the gradient of the last tsr_mlp_grad */
+int      tsr_mlp_adamw_step(tsr_mlp* mlp, float lr, float weight_decay);
+
+/* ---- learned closure in the two-scale system (no reference counterpart) --
+ * For a context built with tsr_model_ext.cell_learned (one scenario,
+ * model_type 3).  Learned cells carry one unknown (interior mean water
+ * content) and use the closure coefficients; the others keep their micro
+ * meshes and the plain FP64 cell kernel. */
+/* new learned/micro assignment of the cells ([no_elements] 0/1); the state
+ * is re-laid out on the device (micro -> learned: interior mean water
+ * content; learned -> micro: the head of that content on every node) */
+int tsr_closure_set_learned(tsr_ctx* ctx, const int* learned);
+/* closure coefficients (kQ, kT) of every cell, 2 * no_elements doubles */
+int tsr_closure_set_coef(tsr_ctx* ctx, const double* kappa);
+/* current assignment, coefficients and indicator flags (each may be NULL) */
+int tsr_closure_read(tsr_ctx* ctx, int* learned, double* kappa, int* flags);
+/* attach the network: norm = feature means [6], feature std [6], output
+ * means [2], output std [2]; zrange = accepted standardised feature range,
+ * low [6] then high [6]; thr = indicator threshold on the relative change
+ * of the exchange flux, qfloor = flux floor of that ratio; auto_fallback:
+ * flagged cells return to their micro meshes before the next step */
+int tsr_closure_attach(tsr_ctx* ctx, tsr_mlp* mlp, const double* norm, const float* zrange,
+                       double thr, double qfloor, int auto_fallback);
+/* coefficients of the learned cells at the loaded state and the indicator */
+int tsr_closure_update(tsr_ctx* ctx, int* n_flagged);
+/* one accepted EXPREM step with the closure (update, fallback, step) */
+int tsr_closure_advance(tsr_ctx* ctx, double tend, const double* tspan, double* tspan_solns,
+                        const exprem_options_struct* options, exprem_stats_struct* stats,
+                        double* t_out, int* n_fallback);
+/* per-cell summary of u (NULL: the loaded state): H_c, theta, d theta/dt,
+ * Q, h(theta) -- 5 doubles per cell (the training data of the network) */
+int tsr_cell_summary(tsr_ctx* ctx, const double* u, double* out);
+
 /* ---- measurement hooks (no reference counterpart) ---------------------- */
 
 /* Enable (1) or disable (0) CUDA-event timing of the kernel classes inside

@@ -44,6 +44,8 @@ def load(libm=False):
         _sig(lib, "oracle_jv", C.c_int, [vp, dp, dp, dp, C.c_double, dp, C.c_int])
         _sig(lib, "oracle_water", C.c_int, [vp, dp, dp])
         _sig(lib, "oracle_water_scenarios", C.c_int, [vp, dp, dp])
+        _sig(lib, "oracle_cell_summary", C.c_int, [vp, dp, dp, dp])
+        _sig(lib, "oracle_vg_head", C.c_double, [C.POINTER(capi.Soil), C.c_double])
         _sig(lib, "oracle_dot", C.c_double, [dp, dp, C.c_long])
         _sig(lib, "oracle_vsum", C.c_double, [dp, C.c_long])
         _sig(lib, "oracle_wsq", C.c_double, [dp, dp, C.c_long])
@@ -118,6 +120,11 @@ class Oracle:
         w = np.empty(self.p.S)
         self.lib.oracle_water_scenarios(self.h, self._p(u), self._p(w))
         return w
+
+    def cell_summary(self, u, g):
+        out = np.empty(5 * self.p.Ne)
+        self.lib.oracle_cell_summary(self.h, self._p(u), self._p(g), self._p(out))
+        return out.reshape(self.p.Ne, 5)
 
     def dot(self, x, y):
         return self.lib.oracle_dot(self._p(x), self._p(y), x.size)

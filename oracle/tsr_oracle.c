@@ -128,6 +128,20 @@ static void vg_eval(double h, const vgpar* p, double* K, double* Cn, double* Cd,
     }
 }
 
+/* Head of material p at water content theta (inverse of the retention
+ * curve): Se = (theta - thr) / dth, h = -((Se^(-1/m) - 1)^(1/n)) / alpha,
+ * 0 at or above saturation, Se floored at 1e-12. */
+static double vg_head(double theta, const vgpar* p)
+{
+    double Se = (theta - p->thr) / p->dth;
+    if (!(Se < 1.0)) return 0.0;
+    if (!(Se > 1e-12)) Se = 1e-12;
+    double L = tsr_log(Se, &T);
+    double tt = tsr_expm1(-(L / p->m), &T);
+    double lt = tsr_log(tt, &T);
+    return -(tsr_exp(lt / p->n, &T) / p->alpha);
+}
+
 /* ------------------------------------------------------------------ */
 /* Effective conductivity Keff(h) (include/Keff.h:1-8; table layout of
  * src/read_effective_conductivity.cpp:52-56): linear interpolation in
@@ -291,6 +305,9 @@ typedef struct oracle_problem {
     long* scen_start;           /* [S+1] */
     vgpar* scen_pA;             /* [S] or NULL (all pA) */
     double* scen_kscale;        /* [S] or NULL (all 1) */
+    /* learned closure: cells with learned[k] carry one unknown */
+    const int* learned;         /* [Ne] or NULL */
+    const double* kappa;        /* [2 Ne] or NULL */
     long N;
     int Mn, Ne, nv, mn, mNe;
     /* EXPREM workspace */
@@ -339,6 +356,8 @@ oracle_problem* oracle_create(const user_data_struct* ud, const tsr_model_ext* e
     P->S = (ext && ext->scenarios > 1) ? ext->scenarios : 1;
     P->scen_nodes = P->Mn / P->S;
     P->scen_cells = P->Ne / P->S;
+    P->learned = ext ? ext->cell_learned : NULL;
+    P->kappa = ext ? ext->closure_coef : NULL;
     P->cell_off = (long*)malloc(sizeof(long) * (size_t)(P->Ne > 0 ? P->Ne : 1));
     P->node_off = (long*)malloc(sizeof(long) * (size_t)(P->Mn > 0 ? P->Mn : 1));
     P->scen_start = (long*)malloc(sizeof(long) * (size_t)(P->S + 1));
@@ -348,7 +367,7 @@ oracle_problem* oracle_create(const user_data_struct* ud, const tsr_model_ext* e
         for (int i = s * P->scen_nodes; i < (s + 1) * P->scen_nodes; ++i) P->node_off[i] = off++;
         for (int k = s * P->scen_cells; k < (s + 1) * P->scen_cells; ++k) {
             P->cell_off[k] = off;
-            off += P->tpl[P->cell_tpl ? P->cell_tpl[k] : 0].no_nodes;
+            off += (P->learned && P->learned[k]) ? 1 : P->tpl[P->cell_tpl ? P->cell_tpl[k] : 0].no_nodes;
         }
     }
     P->scen_start[P->S] = off;
@@ -486,6 +505,17 @@ static double micro_cell(const oracle_problem* P, const double* x, int k, double
     double al[4];
     interp_coeffs(P, x, k, al);
     const double cx = M->centroid_elements[k], cy = M->centroid_elements[Ne + k];
+    if (P->learned && P->learned[k]) {
+        /* learned closure: one unknown, the interior mean water content */
+        const double th = x[off];
+        const double hb = vg_head(th, pB);
+        const double Hc = interp_at(P->nv, al, cx, cy);
+        const double d = Hc - hb;
+        const double kQ = P->kappa ? P->kappa[2 * k] : 0.0;
+        const double kT = P->kappa ? P->kappa[2 * k + 1] : 0.0;
+        g[off] = kT * d;
+        return kQ * d;
+    }
     for (int l = 0; l < mn; ++l) {
         double hl;
         if (m->boundary_nodes[l] == 1) {
@@ -730,6 +760,9 @@ static int water_terms(oracle_problem* P, const double* u, double* water, double
                     py = fma(s, m->vectors[mn + l], cy);
                 }
                 hl = interp_at(nv, al, px, py);
+            } else if (P->learned && P->learned[k]) {
+                p[l & 31] += u[P->cell_off[k]] * m->CV_area[l];
+                continue;
             } else {
                 hl = u[P->cell_off[k] + l];
             }
@@ -1119,6 +1152,64 @@ int oracle_exprem_step(oracle_problem* P, double* t_io, double tend, const doubl
 
 /* ------------------------------------------------------------------ */
 /* elementary functions, exported for their tests */
+/* Per-cell summary of state u with g = G(u) (5 doubles per cell): macro
+ * head at the cell centre H_c, interior mean water content theta (weights
+ * CV areas), its rate sum C(h) g A / sum A, the exchange inflow Q and the
+ * head h(theta) of the inverse retention curve.  Lane-ordered sums (item l
+ * to lane l mod 32, then the xor butterfly).  Learned cells report their
+ * unknown and closure values. */
+int oracle_cell_summary(oracle_problem* P, const double* u, const double* g, double* out)
+{
+    const macro_mesh_struct* M = &P->ud.macro_mesh;
+    const int Ne = P->Ne;
+    double* gs = (double*)malloc(sizeof(double) * (size_t)P->N);
+    double* scratch = (double*)malloc(sizeof(double) * scratch_doubles(P));
+    for (int k = 0; k < Ne; ++k) {
+        const micro_mesh_struct* m = &P->tpl[P->cell_tpl ? P->cell_tpl[k] : 0];
+        const vgpar* pB = P->cell_pB ? &P->cell_pB[k] : &P->pB;
+        double al[4];
+        interp_coeffs(P, u, k, al);
+        const double Hc = interp_at(P->nv, al, M->centroid_elements[k], M->centroid_elements[Ne + k]);
+        const double Q = micro_cell(P, u, k, gs, scratch);
+        double th, rate;
+        if (P->learned && P->learned[k]) {
+            th = u[P->cell_off[k]];
+            rate = g[P->cell_off[k]];
+        } else {
+            double pw[32], pt[32], pr[32];
+            for (int l = 0; l < 32; ++l) pw[l] = pt[l] = pr[l] = 0.0;
+            for (int l = 0; l < m->no_nodes; ++l) {
+                if (m->boundary_nodes[l] == 1) continue;
+                const double h = u[P->cell_off[k] + l];
+                double K, Cn, Cd, Se;
+                vg_eval(h, pB, &K, &Cn, &Cd, &Se);
+                const double A = m->CV_area[l];
+                pw[l & 31] += A;
+                pt[l & 31] += fma(pB->dth, Se, pB->thr) * A;
+                pr[l & 31] += ((Cn / Cd) * g[P->cell_off[k] + l]) * A;
+            }
+            const double W = butterfly32(pw);
+            th = butterfly32(pt) / W;
+            rate = butterfly32(pr) / W;
+        }
+        double* o = out + (size_t)5 * k;
+        o[0] = Hc;
+        o[1] = th;
+        o[2] = rate;
+        o[3] = Q;
+        o[4] = vg_head(th, pB);
+    }
+    free(gs);
+    free(scratch);
+    return 0;
+}
+
+double oracle_vg_head(const soil_struct* s, double theta)
+{
+    vgpar p = make_vgpar(s);
+    return vg_head(theta, &p);
+}
+
 double oracle_math_log(double x) { return tsr_log(x, &T); }
 double oracle_math_exp(double x) { return tsr_exp(x, &T); }
 double oracle_math_expm1(double x) { return tsr_expm1(x, &T); }

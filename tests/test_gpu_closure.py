@@ -1,0 +1,193 @@
+"""The learned closure on the GPU, through the C-ABI.
+
+* The tensor-core network: the fused inference kernel against the
+  layer-by-layer training path (same BF16 rounding points, same mma
+  sequence: equal outputs) and against the CPU oracle (BF16-emulating,
+  FP64 accumulation); its gradient against the oracle's; training lowers
+  the loss.
+* Learned cells inside G, Jv and EXPREM against the oracle, bit for bit,
+  on a mixed layout with given coefficients; the cell summary (training
+  data) against the oracle; the device re-layout against the oracle's
+  summary.
+* End to end on the 21 x 21 configuration: a network trained on plain-run
+  data, the closure run against the plain run, and the ablation against
+  the untrained network.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle
+from oracle import mlp as om
+from twoscalerich_gb300 import capi, closure
+from twoscalerich_gb300 import problem as P
+
+pytestmark = pytest.mark.gpu
+
+
+def _x(n, seed):
+    rng = np.random.default_rng(seed)
+    x = np.zeros((n, 8), dtype=np.float32)
+    x[:, :6] = rng.standard_normal((n, 6)).astype(np.float32)
+    return x
+
+
+def test_mlp_fused_equals_layered_and_oracle():
+    params = om.init_params(11)
+    net = closure.Mlp(params)
+    x = _x(1000, 1)                       # not a multiple of 16 rows
+    yf = net.forward(x, fused=True)
+    yl = net.forward(x, fused=False)
+    assert np.array_equal(yf, yl)
+    yo, _ = om.forward(params, x, bf=True)
+    # FP32 accumulation and the fast exponential can move an activation
+    # across a BF16 rounding boundary (a 2^-8 relative step) where the FP64
+    # oracle does not: rare, and bounded by the BF16 resolution
+    d = np.abs(yf - yo) / np.max(np.abs(yo))
+    assert np.max(d) < 2e-3 and np.median(d) < 1e-5, (np.max(d), np.median(d))
+    net.close()
+
+
+def test_mlp_gradient_matches_oracle():
+    params = om.init_params(12)
+    net = closure.Mlp(params)
+    x = _x(777, 2)
+    y = np.random.default_rng(3).standard_normal((777, 2)).astype(np.float32)
+    loss, g = net.grad(x, y)
+    lo, go = om.loss_grad(params, x, y, bf=True)
+    assert abs(loss - lo) <= 1e-5 * abs(lo)
+    for (w, b, no, ni) in om.LAYOUT:
+        for sl in (slice(w, b), slice(b, b + no)):
+            ref = go[sl]
+            assert np.linalg.norm(g[sl] - ref) <= 2e-3 * np.linalg.norm(ref) + 1e-9, (w, b)
+    # the plain FP64 gradient agrees to the BF16 level
+    _, g64 = om.loss_grad(params.astype(np.float64), x.astype(np.float64), y.astype(np.float64), bf=False)
+    assert np.linalg.norm(g - g64) <= 5e-2 * np.linalg.norm(g64)
+    net.close()
+
+
+def test_mlp_training_lowers_loss():
+    rng = np.random.default_rng(4)
+    x = _x(20000, 5)
+    y = np.column_stack([np.sin(x[:, 0]) + 0.5 * x[:, 1], x[:, 2] * x[:, 3]]).astype(np.float32)
+    net = closure.Mlp(closure.init_params(1001))
+    l0 = float(np.mean((net.forward(x) - y) ** 2))
+    hist = net.train(x, y, epochs=6, batch=1024, lr=3e-3, seed=1001)
+    l1 = float(np.mean((net.forward(x) - y) ** 2))
+    assert hist[-1] < hist[0] and l1 < 0.2 * l0, (hist, l0, l1)
+    net.close()
+
+
+def _mixed_problem():
+    p = P.config1()
+    rng = np.random.default_rng(3)
+    learned = (rng.uniform(size=p.Ne) < 0.5).astype(np.int32)
+    kappa = np.column_stack([rng.uniform(0.001, 0.01, p.Ne), rng.uniform(0.1, 1.0, p.Ne)]).ravel()
+    p.set_learned(learned, kappa)
+    return p, learned, kappa
+
+
+def _mixed_state(p, learned, seed=4):
+    rng = np.random.default_rng(seed)
+    u = p.u0[:p.N].copy() if p.u0.size >= p.N else np.full(p.N, -5.0)
+    u = -2.0 + rng.uniform(-0.5, 0.5, p.N)
+    soil = P.make_soil(**P.SOIL_B)
+    lib = oracle.load()
+    for k in np.flatnonzero(learned):
+        u[p.cell_off[k]] = 0.25 + rng.uniform(-0.01, 0.01)
+    u[p.node_off[p.dirichlet_nodes]] = p.dirichlet_h
+    return u
+
+
+def test_learned_cells_g_jv_summary_bitwise():
+    p, learned, kappa = _mixed_problem()
+    ctx = P.Context(p)
+    orc = oracle.Oracle(p, nthreads=4)
+    u = _mixed_state(p, learned)
+    v = np.random.default_rng(7).standard_normal(p.N)
+    g = ctx.g(u)
+    go = orc.g(u)
+    assert np.array_equal(g, go)
+    assert np.array_equal(ctx.jv(u, g, v, 2e-8), orc.jv(u, go, v, 2e-8))
+    assert ctx.water(u) == orc.water(u)
+    out = np.empty(5 * p.Ne)
+    capi.check(ctx.lib.tsr_cell_summary(ctx.h, capi.ptr(u), capi.ptr(out)), "summary")
+    assert np.array_equal(out.reshape(p.Ne, 5), orc.cell_summary(u, go))
+
+
+def test_learned_cells_exprem_trajectory_bitwise():
+    p, learned, kappa = _mixed_problem()
+    p.u0 = _mixed_state(p, learned, seed=9)
+    p.tend = 0.05
+    p.tspan = np.array([1.0, 0.05])
+    ctx = P.Context(p)
+    orc = oracle.Oracle(p, nthreads=4)
+    ug, sg, stg, logg = P.run_to_end(ctx.exprem_step, p)
+    uo, so, sto, logo = P.run_to_end(orc.exprem_step, p)
+    assert logg == logo
+    assert np.array_equal(ug, uo) and np.array_equal(sg, so)
+
+
+def test_relayout_matches_oracle_summary():
+    p = P.config1()
+    p.set_learned(np.zeros(p.Ne, dtype=np.int32))
+    ctx = P.Context(p)
+    lib = ctx.lib
+    u = p.u0 + np.random.default_rng(2).uniform(-0.4, 0.4, p.N)
+    orc = oracle.Oracle(p, nthreads=4)
+    S = orc.cell_summary(u, orc.g(u))
+    capi.check(lib.tsr_exprem_load(ctx.h, capi.ptr(u), 0.0), "load")
+    learned = np.zeros(p.Ne, dtype=np.int32)
+    learned[::3] = 1
+    capi.check(lib.tsr_closure_set_learned(ctx.h, learned.ctypes.data_as(capi.ip)), "relayout")
+    n = lib.tsr_num_unknowns(ctx.h)
+    assert n == p.Mn + learned.sum() + (1 - learned).sum() * p.mn
+    v = np.empty(n)
+    capi.check(lib.tsr_exprem_store(ctx.h, capi.ptr(v)), "store")
+    q = P.config1()
+    q.set_learned(learned)
+    assert np.array_equal(v[:p.Mn], u[:p.Mn])
+    for k in range(p.Ne):
+        if learned[k]:
+            assert v[q.cell_off[k]] == S[k, 1]
+        else:
+            a = p.cell_off[k]
+            assert np.array_equal(v[q.cell_off[k]:q.cell_off[k] + p.mn], u[a:a + p.mn])
+    # and back: every node of a re-resolved cell at the head of its content
+    capi.check(lib.tsr_closure_set_learned(ctx.h, np.zeros(p.Ne, dtype=np.int32).ctypes.data_as(capi.ip)),
+               "relayout back")
+    w = np.empty(p.N)
+    capi.check(lib.tsr_exprem_store(ctx.h, capi.ptr(w)), "store")
+    soil = P.make_soil(**P.SOIL_B)
+    olib = oracle.load()
+    for k in np.flatnonzero(learned)[:20]:
+        hb = olib.oracle_vg_head(C.byref(soil), S[k, 1])
+        assert np.all(w[p.cell_off[k]:p.cell_off[k] + p.mn] == hb)
+
+
+@pytest.mark.slow
+def test_closure_end_to_end_and_ablation():
+    """Train on plain runs of the 21 x 21 / 11 x 11 configuration (training
+    initial states from seeds 1001-1003), evaluate on the evaluation
+    state, compare with the plain run and with the untrained network."""
+    X, Y = [], []
+    for seed in (1001, 1002, 1003):
+        q = P.config1()
+        q.u0 = q.initial_state(-5.0, noise=0.2, seed=seed)
+        logs = closure.log_plain_run(q)
+        x, y = closure.samples(q, logs)
+        X.append(x)
+        Y.append(y)
+    X, Y = np.concatenate(X), np.concatenate(Y)
+    model, hist, err = closure.train_model(X, Y, epochs=6, batch=2048, lr=2e-3, seed=1001)
+    assert hist[-1] < hist[0]
+    times = [0.25, 0.5, 1.0]
+    plain, wp, sp, fp, = P.config1(), None, None, None
+    rec_p, wall_p, steps_p, evals_p = closure.run_plain(plain, times)
+    rec_c, wall_c, steps_c, evals_c, frac = closure.run_closure(P.config1(), model, times)
+    rec_u, *_ = closure.run_closure(P.config1(), model, times, params=closure.init_params(7))
+    ep = [abs(c[1] - r[1]) / r[1] for c, r in zip(rec_c, rec_p)]
+    eu = [abs(c[1] - r[1]) / r[1] for c, r in zip(rec_u, rec_p)]
+    assert max(ep) < 1e-2, ep
+    assert max(ep) < max(eu), (ep, eu)

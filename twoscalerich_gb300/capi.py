@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(HERE, "libtsr_gb300.so")
 
 dp = C.POINTER(C.c_double)
 ip = C.POINTER(C.c_int)
+fp = C.POINTER(C.c_float)
 
 
 class MacroMesh(C.Structure):
@@ -86,6 +87,7 @@ class ModelExt(C.Structure):
         ("templates", C.POINTER(MicroMesh)), ("cell_template", ip),
         ("cell_soilB", C.POINTER(Soil)), ("scenarios", C.c_int), ("reserved2", C.c_int),
         ("scen_soilA", C.POINTER(Soil)), ("scen_keff_scale", dp),
+        ("cell_learned", ip), ("closure_coef", dp),
     ]
 
 
@@ -150,6 +152,24 @@ _SIGNATURES = {
     "tsr_sync": (C.c_int, [C.c_void_p]),
     "tsr_pinned_alloc": (C.c_void_p, [C.c_size_t]),
     "tsr_pinned_free": (None, [C.c_void_p]),
+    "tsr_mlp_num_params": (C.c_int, []),
+    "tsr_mlp_create": (C.c_void_p, []),
+    "tsr_mlp_free": (None, [C.c_void_p]),
+    "tsr_mlp_set_params": (C.c_int, [C.c_void_p, fp]),
+    "tsr_mlp_get_params": (C.c_int, [C.c_void_p, fp]),
+    "tsr_mlp_forward": (C.c_int, [C.c_void_p, fp, C.c_int, fp, C.c_int]),
+    "tsr_mlp_grad": (C.c_int, [C.c_void_p, fp, fp, C.c_int, fp, fp]),
+    "tsr_mlp_set_data": (C.c_int, [C.c_void_p, fp, fp, C.c_longlong]),
+    "tsr_mlp_train": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_ulonglong, fp]),
+    "tsr_mlp_adamw_step": (C.c_int, [C.c_void_p, C.c_float, C.c_float]),
+    "tsr_closure_set_learned": (C.c_int, [C.c_void_p, ip]),
+    "tsr_closure_set_coef": (C.c_int, [C.c_void_p, dp]),
+    "tsr_closure_read": (C.c_int, [C.c_void_p, ip, dp, ip]),
+    "tsr_closure_attach": (C.c_int, [C.c_void_p, C.c_void_p, dp, fp, C.c_double, C.c_double, C.c_int]),
+    "tsr_closure_update": (C.c_int, [C.c_void_p, ip]),
+    "tsr_closure_advance": (C.c_int, [C.c_void_p, C.c_double, dp, dp, C.POINTER(ExpremOptions),
+                                      C.POINTER(ExpremStats), dp, ip]),
+    "tsr_cell_summary": (C.c_int, [C.c_void_p, dp, dp]),
     "tsr_dot_device_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p,
                                          C.c_void_p]),
 }

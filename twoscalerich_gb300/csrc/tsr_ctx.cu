@@ -112,6 +112,26 @@ struct tsr_ctx {
     std::vector<std::array<cudaEvent_t, 4>> graph_ev;
     double prof_acc_ms[2] = {0.0, 0.0}, prof_acc_bytes[2] = {0.0, 0.0};
     long long prof_acc_n[2] = {0, 0};
+    // learned closure: cell layout that changes between steps
+    bool closure = false;
+    long long N_cap = 0;                 // unknowns with every cell resolved (buffer capacity)
+    int pseudo_tpl = -1;                 // template index of learned cells
+    std::vector<int> tpl_full_host;      // [Ne] micro template of every cell
+    std::vector<int> learned_host;       // [Ne]
+    std::vector<long long> tpl_nodes;    // nodes of each micro template
+    long long* d_off[2] = {nullptr, nullptr};
+    int* d_learned[2] = {nullptr, nullptr};
+    int cur = 0;                         // current layout buffer
+    int* d_cell_tpl = nullptr;
+    int* d_lcells = nullptr;             // [Ne] learned cells
+    int nl = 0;
+    double *d_kappa = nullptr, *d_hist = nullptr, *d_hcur = nullptr, *d_summary = nullptr, *d_qlog = nullptr;
+    double* d_aint = nullptr;
+    int *d_hcount = nullptr, *d_flags = nullptr, *d_nflag = nullptr;
+    double thist[3] = {0.0, 0.0, 0.0};
+    tsr_mlp* mlp = nullptr;
+    ClosureDev cdev{};
+    bool auto_fallback = true;
 };
 
 namespace {
@@ -324,10 +344,18 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
                     return TSR_ERR_ARG;
                 }
     c->S = nscen;
+    c->closure = ext && ext->cell_learned;
+    if (c->closure && (nscen > 1 || ud.model_type != 3)) {
+        set_error("the learned closure needs one scenario and model_type 3");
+        return TSR_ERR_ARG;
+    }
+    c->pseudo_tpl = c->closure ? ntpl : -1;
     c->cell_tpl_host.assign((size_t)Ne, 0);
+    c->tpl_full_host.assign((size_t)Ne, 0);
+    c->learned_host.assign((size_t)Ne, 0);
     std::vector<long long> cell_off((size_t)Ne), node_off((size_t)Mn);
     c->scen_start.assign((size_t)nscen + 1, 0);
-    long long N = 0;
+    long long N = 0, Ncap = Mn;
     for (int sc = 0; sc < nscen; ++sc) {
         c->scen_start[sc] = N;
         for (int i = sc * sn; i < (sc + 1) * sn; ++i) node_off[i] = N++;
@@ -337,17 +365,26 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
                 set_error("cell_template out of range");
                 return TSR_ERR_BOUNDS;
             }
-            c->cell_tpl_host[k] = t;
+            const bool lk = c->closure && ext->cell_learned[k];
+            c->tpl_full_host[k] = t;
+            c->learned_host[k] = lk ? 1 : 0;
+            c->cell_tpl_host[k] = lk ? c->pseudo_tpl : t;
             cell_off[k] = N;
-            N += tpls[t].no_nodes;
+            N += lk ? 1 : tpls[t].no_nodes;
+            Ncap += tpls[t].no_nodes;
         }
     }
     c->scen_start[nscen] = N;
+    c->N_cap = c->closure ? Ncap : N;
+    if (Ncap > 0x7fffffffLL) {
+        set_error("problem too large for 32-bit indices");
+        return TSR_ERR_ARG;
+    }
     if (N > 0x7fffffffLL || (long long)Ne * 32 > 0x7fffffffLL) {
         set_error("problem too large for 32-bit indices");
         return TSR_ERR_ARG;
     }
-    if (ud.N != 0 && ud.N != (int)N) {
+    if (ud.N != 0 && ud.N != (int)N && !(c->closure && ud.N == (int)Ncap)) {
         set_error("user_data.N does not match the meshes");
         return TSR_ERR_ARG;
     }
@@ -531,6 +568,21 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
             for (int l = 0; l < 2 * mn; ++l) vec.push_back(m.vectors[l]);
             c->tpl_host.push_back(d);
         }
+        c->tpl_nodes.assign((size_t)ntpl, 0);
+        std::vector<double> aint((size_t)ntpl + 1, 0.0);
+        for (int t = 0; t < ntpl; ++t) {
+            c->tpl_nodes[t] = tpls[t].no_nodes;
+            for (int l = 0; l < tpls[t].no_nodes; ++l)
+                if (tpls[t].boundary_nodes[l] != 1) aint[t] += tpls[t].CV_area[l];
+        }
+        if (c->closure) {
+            // learned cells: a template of one unknown and no micro mesh
+            TplDesc d{};
+            d.mn = 1;
+            d.state = 2;
+            d.kind = 1;
+            c->tpl_host.push_back(d);
+        }
         const TplDesc* dt;
         if ((rc = upload(c, c->tpl_host.data(), c->tpl_host.size(), &dt))) return rc;
         S.tpl = dt;
@@ -545,8 +597,59 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
         if ((rc = upload(c, ebc.data(), ebc.size(), &S.eb_count))) return rc;
         if ((rc = upload(c, bv.data(), bv.size(), &S.b_v))) return rc;
         if ((rc = upload(c, bn.data(), bn.size(), &S.b_n))) return rc;
-        if ((rc = upload(c, cell_off.data(), cell_off.size(), &S.cell_off))) return rc;
-        if ((rc = upload(c, c->cell_tpl_host.data(), c->cell_tpl_host.size(), &S.cell_tpl))) return rc;
+        void* q;
+        for (int b = 0; b < (c->closure ? 2 : 1); ++b) {
+            if ((rc = dev_alloc(c, sizeof(long long) * (size_t)(Ne > 0 ? Ne : 1), &q))) return rc;
+            c->d_off[b] = (long long*)q;
+            if ((rc = dev_alloc(c, sizeof(int) * (size_t)(Ne > 0 ? Ne : 1), &q))) return rc;
+            c->d_learned[b] = (int*)q;
+        }
+        c->cur = 0;
+        CK(cudaMemcpy(c->d_off[0], cell_off.data(), sizeof(long long) * (size_t)Ne, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(c->d_learned[0], c->learned_host.data(), sizeof(int) * (size_t)Ne, cudaMemcpyHostToDevice));
+        S.cell_off = c->d_off[0];
+        if ((rc = dev_alloc(c, sizeof(int) * (size_t)(Ne > 0 ? Ne : 1), &q))) return rc;
+        c->d_cell_tpl = (int*)q;
+        CK(cudaMemcpy(c->d_cell_tpl, c->cell_tpl_host.data(), sizeof(int) * (size_t)Ne, cudaMemcpyHostToDevice));
+        S.cell_tpl = c->d_cell_tpl;
+        if ((rc = upload(c, c->tpl_full_host.data(), c->tpl_full_host.size(), &S.cell_tpl_full))) return rc;
+        const double* da;
+        if ((rc = upload(c, aint.data(), aint.size(), &da))) return rc;
+        c->d_aint = const_cast<double*>(da);
+        S.kappa = nullptr;
+        if (c->closure) {
+            const size_t n2 = 2 * (size_t)Ne;
+            if ((rc = dev_alloc(c, sizeof(double) * n2, &q))) return rc;
+            c->d_kappa = (double*)q;
+            if (ext->closure_coef)
+                CK(cudaMemcpy(c->d_kappa, ext->closure_coef, sizeof(double) * n2, cudaMemcpyHostToDevice));
+            else
+                CK(cudaMemset(c->d_kappa, 0, sizeof(double) * n2));
+            S.kappa = c->d_kappa;
+            if ((rc = dev_alloc(c, sizeof(double) * 3 * (size_t)Ne, &q))) return rc;
+            c->d_hist = (double*)q;
+            if ((rc = dev_alloc(c, sizeof(double) * (size_t)Ne, &q))) return rc;
+            c->d_hcur = (double*)q;
+            if ((rc = dev_alloc(c, sizeof(int) * (size_t)Ne, &q))) return rc;
+            c->d_hcount = (int*)q;
+            CK(cudaMemset(c->d_hcount, 0, sizeof(int) * (size_t)Ne));
+            if ((rc = dev_alloc(c, sizeof(int) * (size_t)Ne, &q))) return rc;
+            c->d_flags = (int*)q;
+            CK(cudaMemset(c->d_flags, 0, sizeof(int) * (size_t)Ne));
+            if ((rc = dev_alloc(c, sizeof(int) * 4, &q))) return rc;
+            c->d_nflag = (int*)q;
+            if ((rc = dev_alloc(c, sizeof(int) * (size_t)Ne, &q))) return rc;
+            c->d_lcells = (int*)q;
+            std::vector<int> lc;
+            for (int k = 0; k < Ne; ++k)
+                if (c->learned_host[k]) lc.push_back(k);
+            c->nl = (int)lc.size();
+            if (c->nl) CK(cudaMemcpy(c->d_lcells, lc.data(), sizeof(int) * lc.size(), cudaMemcpyHostToDevice));
+        }
+        if ((rc = dev_alloc(c, sizeof(double) * 5 * (size_t)(Ne > 0 ? Ne : 1), &q))) return rc;
+        c->d_summary = (double*)q;
+        if ((rc = dev_alloc(c, sizeof(double) * (size_t)(Ne > 0 ? Ne : 1), &q))) return rc;
+        c->d_qlog = (double*)q;
         S.cell_par = nullptr;
         if (ext && ext->cell_soilB) {
             std::vector<VGPar> par((size_t)Ne);
@@ -608,7 +711,7 @@ int make_seg(tsr_ctx* c, const std::vector<long long>& start, SegInfo* g)
 
 int alloc_work(tsr_ctx* c, int max_krylov)
 {
-    const long long N = c->N;
+    const long long N = c->N_cap;   // buffers hold the largest cell layout
     const int S = c->S;
     void* p;
     int rc;
@@ -1708,5 +1811,212 @@ extern "C" int tsr_set_graphs(tsr_ctx* c, int enable)
 {
     if (!c) return TSR_ERR_ARG;
     c->use_graphs = enable != 0;
+    return TSR_OK;
+}
+
+// ---- learned closure ------------------------------------------------------------
+// Cells switch between the micro mesh (plain FP64 cell kernel) and the
+// learned closure between steps; the unknown vector is re-laid out on the
+// device and the Arnoldi graphs are captured again.
+
+namespace {
+
+int relayout(tsr_ctx* c, const std::vector<int>& learned_new)
+{
+    const int Ne = c->Ne, Mn = c->Mn;
+    Problem& P = c->P;
+    cudaStream_t s = c->stream;
+    // interior mean water content of the cells that become learned
+    launch_cell_summary(P, c->d_u, nullptr, nullptr, c->d_summary, s);
+    std::vector<long long> off((size_t)Ne);
+    long long N = Mn;
+    std::vector<int> lc;
+    for (int k = 0; k < Ne; ++k) {
+        off[k] = N;
+        N += learned_new[k] ? 1 : c->tpl_nodes[c->tpl_full_host[k]];
+        c->cell_tpl_host[k] = learned_new[k] ? c->pseudo_tpl : c->tpl_full_host[k];
+        if (learned_new[k]) lc.push_back(k);
+    }
+    const int nb = 1 - c->cur;
+    CK(cudaStreamSynchronize(s));
+    CK(cudaMemcpyAsync(c->d_off[nb], off.data(), sizeof(long long) * (size_t)Ne, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(c->d_learned[nb], learned_new.data(), sizeof(int) * (size_t)Ne, cudaMemcpyHostToDevice, s));
+    launch_relayout(P, Mn, Ne, c->d_off[c->cur], c->d_learned[c->cur], c->d_off[nb], c->d_learned[nb],
+                    c->d_summary, c->d_u, c->d_unew, s);
+    CK(cudaGetLastError());
+    // cells that become learned start a new head history
+    std::vector<int> fresh;
+    for (int k = 0; k < Ne; ++k)
+        if (learned_new[k] && !c->learned_host[k]) fresh.push_back(k);
+    CK(cudaMemcpyAsync(c->d_cell_tpl, c->cell_tpl_host.data(), sizeof(int) * (size_t)Ne, cudaMemcpyHostToDevice, s));
+    if (!lc.empty())
+        CK(cudaMemcpyAsync(c->d_lcells, lc.data(), sizeof(int) * lc.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    if (!fresh.empty()) {
+        std::vector<int> hc((size_t)Ne);
+        CK(cudaMemcpy(hc.data(), c->d_hcount, sizeof(int) * (size_t)Ne, cudaMemcpyDeviceToHost));
+        for (int k : fresh) hc[k] = 0;
+        CK(cudaMemcpy(c->d_hcount, hc.data(), sizeof(int) * (size_t)Ne, cudaMemcpyHostToDevice));
+    }
+    std::swap(c->d_u, c->d_unew);
+    c->cur = nb;
+    c->learned_host = learned_new;
+    c->nl = (int)lc.size();
+    P.m.cell_off = c->d_off[nb];
+    c->N = N;
+    P.N = N;
+    c->scen_start[1] = N;
+    int rc;
+    if ((rc = make_seg(c, c->scen_start, &c->seg))) return rc;
+    c->sc[0].g0_valid = false;
+    return tsr::plan_cells(c, c->tuned_threads, c->tuned_budget);
+}
+
+ClosureDev closure_dev(tsr_ctx* c)
+{
+    ClosureDev C = c->cdev;
+    C.w = mlp_device_weights(c->mlp);
+    C.p = mlp_device_params(c->mlp);
+    C.cells = c->d_lcells;
+    C.n = c->nl;
+    C.hist = c->d_hist;
+    C.hcount = c->d_hcount;
+    C.hcur = c->d_hcur;
+    C.t[0] = c->sc[0].t;
+    C.t[1] = c->thist[0];
+    C.t[2] = c->thist[1];
+    C.t[3] = c->thist[2];
+    C.kappa = c->d_kappa;
+    C.aint = c->d_aint;
+    C.flags = c->d_flags;
+    C.nflag = c->d_nflag;
+    return C;
+}
+
+}  // namespace
+
+extern "C" int tsr_closure_set_learned(tsr_ctx* c, const int* learned)
+{
+    if (!c || !learned) return TSR_ERR_ARG;
+    if (!c->closure) {
+        set_error("context built without the learned closure (tsr_model_ext.cell_learned)");
+        return TSR_ERR_ARG;
+    }
+    std::vector<int> l((size_t)c->Ne);
+    for (int k = 0; k < c->Ne; ++k) l[k] = learned[k] ? 1 : 0;
+    return relayout(c, l);
+}
+
+extern "C" int tsr_closure_set_coef(tsr_ctx* c, const double* kappa)
+{
+    if (!c || !kappa || !c->closure) return TSR_ERR_ARG;
+    CK(cudaMemcpyAsync(c->d_kappa, kappa, sizeof(double) * 2 * (size_t)c->Ne, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return TSR_OK;
+}
+
+extern "C" int tsr_closure_read(tsr_ctx* c, int* learned, double* kappa, int* flags)
+{
+    if (!c || !c->closure) return TSR_ERR_ARG;
+    const size_t Ne = (size_t)c->Ne;
+    if (learned) std::memcpy(learned, c->learned_host.data(), sizeof(int) * Ne);
+    if (kappa) CK(cudaMemcpyAsync(kappa, c->d_kappa, sizeof(double) * 2 * Ne, cudaMemcpyDeviceToHost, c->stream));
+    if (flags) CK(cudaMemcpyAsync(flags, c->d_flags, sizeof(int) * Ne, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return TSR_OK;
+}
+
+extern "C" int tsr_closure_attach(tsr_ctx* c, tsr_mlp* mlp, const double* norm, const float* zrange, double thr,
+                                  double qfloor, int auto_fallback)
+{
+    if (!c || !mlp || !norm || !zrange || !c->closure) return TSR_ERR_ARG;
+    c->mlp = mlp;
+    ClosureDev& C = c->cdev;
+    for (int i = 0; i < 6; ++i) {
+        C.fmu[i] = norm[i];
+        C.fsd[i] = norm[6 + i];
+        C.zlo[i] = zrange[i];
+        C.zhi[i] = zrange[6 + i];
+    }
+    C.ymu[0] = norm[12];
+    C.ymu[1] = norm[13];
+    C.ysd[0] = norm[14];
+    C.ysd[1] = norm[15];
+    C.thr = thr;
+    C.qfloor = qfloor;
+    c->auto_fallback = auto_fallback != 0;
+    return TSR_OK;
+}
+
+// Coefficients of the learned cells at the current state, and the
+// indicator; returns the number of flagged cells in *n_flagged.
+extern "C" int tsr_closure_update(tsr_ctx* c, int* n_flagged)
+{
+    if (!c || !c->closure || !c->mlp || !c->sc[0].loaded) return TSR_ERR_ARG;
+    CK(cudaMemsetAsync(c->d_nflag, 0, sizeof(int), c->stream));
+    ClosureDev C = closure_dev(c);
+    launch_closure_update(c->P, c->d_u, C, c->stream);
+    CK(cudaGetLastError());
+    int nf = 0;
+    CK(cudaMemcpyAsync(c->h_flag, c->d_nflag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    nf = c->h_flag[0];
+    if (n_flagged) *n_flagged = nf;
+    return TSR_OK;
+}
+
+// One accepted step of the two-scale system with the learned closure:
+// coefficients and indicator at the current state, fallback of the flagged
+// cells to their micro meshes (when enabled), one EXPREM step, head history.
+extern "C" int tsr_closure_advance(tsr_ctx* c, double tend, const double* tspan, double* tspan_solns,
+                                   const exprem_options_struct* opt, exprem_stats_struct* st, double* t_out,
+                                   int* n_fallback)
+{
+    if (!c || !opt || !st || !tspan || !c->closure || !c->sc[0].loaded) return TSR_ERR_ARG;
+    int rc, nf = 0;
+    const bool use = c->mlp && c->nl > 0;
+    if (use) {
+        if ((rc = tsr_closure_update(c, &nf))) return rc;
+        if (nf > 0 && c->auto_fallback) {
+            std::vector<int> flags((size_t)c->Ne);
+            CK(cudaMemcpy(flags.data(), c->d_flags, sizeof(int) * (size_t)c->Ne, cudaMemcpyDeviceToHost));
+            std::vector<int> l = c->learned_host;
+            for (int k = 0; k < c->Ne; ++k)
+                if (l[k] && flags[k]) l[k] = 0;
+            if ((rc = relayout(c, l))) return rc;
+        }
+    }
+    const double t0 = c->sc[0].t;
+    if ((rc = tsr_exprem_advance(c, tend, tspan, tspan_solns, opt, st, t_out))) return rc;
+    if (use && c->nl > 0) {
+        launch_closure_push(closure_dev(c), c->stream);
+        CK(cudaGetLastError());
+        c->thist[2] = c->thist[1];
+        c->thist[1] = c->thist[0];
+        c->thist[0] = t0;
+    }
+    if (n_fallback) *n_fallback = nf;
+    return TSR_OK;
+}
+
+// Per-cell summary of state u (host, current layout; NULL: the loaded
+// state): 5 doubles per cell, H_c, theta, d theta/dt, Q, h(theta).
+extern "C" int tsr_cell_summary(tsr_ctx* c, const double* u, double* out)
+{
+    if (!c || !out || c->S != 1) return TSR_ERR_ARG;
+    int rc;
+    if ((rc = all_active(c))) return rc;
+    const double* du = c->d_u;
+    if (u) {
+        CK(cudaMemcpyAsync(c->d_x, u, sizeof(double) * (size_t)c->N, cudaMemcpyHostToDevice, c->stream));
+        du = c->d_x;
+    }
+    c->P.qlog = c->d_qlog;
+    launch_g(c->P, 0, du, nullptr, nullptr, nullptr, c->d_y, c->stream);
+    c->P.qlog = nullptr;
+    launch_cell_summary(c->P, du, c->d_y, c->d_qlog, c->d_summary, c->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, c->d_summary, sizeof(double) * 5 * (size_t)c->Ne, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
     return TSR_OK;
 }

@@ -6,7 +6,13 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 
+struct tsr_mlp;
+
 namespace tsr {
+
+// the closure network's device parameters (tsr_mlp.cu)
+const void* mlp_device_weights(const tsr_mlp* m);
+const float* mlp_device_params(const tsr_mlp* m);
 
 // Van Genuchten parameters with the derived constants the kernels use.
 struct VGPar {
@@ -21,6 +27,8 @@ struct VGPar {
 struct TplDesc {
     int mn, mNe, nb, state;      // nodes, elements, boundary items, shared doubles per cell
     int ev, eg, csr_ptr, csr_ent, node, bitem;   // offsets (elements, nodes, items)
+    int kind;                    // 0 micro mesh, 1 learned closure (one unknown per cell)
+    int pad;
 };
 
 struct MicroSet {
@@ -47,6 +55,9 @@ struct MicroSet {
     const int* bundle_first;     // [n_bundles] index into bundle_cells
     const int* bundle_count;     // [n_bundles]
     const int* bundle_cells;     // cell ids, grouped by bundle
+    // learned closure
+    const int* cell_tpl_full;    // [Ne] micro template of every cell (geometry of learned cells)
+    const double* kappa;         // [2 Ne] closure coefficients (kQ, kT) per cell
 };
 
 // Macro mesh in the reference layout plus derived arrays.
@@ -96,6 +107,30 @@ struct Problem {
     const int* active;          // [nscen] scenarios to evaluate, or nullptr (all)
     int eps_stride;             // doubles between consecutive scenarios' {eps, 1/eps}
     long long N;
+    double* qlog;               // [Ne] exchange inflow of every cell (plain G), or nullptr
+};
+
+// Learned-closure update of one step: features of the learned cells, the
+// network, the coefficients and the a-posteriori indicator.
+struct ClosureDev {
+    const void* w;              // bf16 weights (parameter-block indexing)
+    const float* p;             // FP32 parameter block (biases)
+    double fmu[6], fsd[6];      // feature standardisation
+    double ymu[2], ysd[2];      // output de-standardisation
+    float zlo[6], zhi[6];       // accepted range of the standardised features
+    const int* cells;           // [n] learned cells
+    int n;
+    int pad;
+    double* hist;               // [3 Ne] macro head at the cell centre, last 3 accepted states
+    int* hcount;                // [Ne] valid history entries
+    double* hcur;               // [Ne] the same at the current state
+    double t[4];                // current time and the 3 previous accepted times
+    double* kappa;              // [2 Ne]
+    const double* aint;         // [ntpl] interior CV area of each template
+    int* flags;                 // [Ne] indicator result
+    int* nflag;                 // device counter
+    double thr;                 // indicator threshold (relative flux change)
+    double qfloor;              // flux floor of the relative measure
 };
 
 // Vector segments (one per scenario) for reductions and elementwise work.
@@ -168,6 +203,21 @@ void add_launches(int n);
 void set_counting(bool on);
 // measured FP64 instruction rate of the device (DFMA chains)
 int measure_fp64_peak(double* ops_per_s);
+
+// per-cell summary (5 doubles: H_c, theta, rate, Q, h(theta)) of state u
+// with g = G(u) (g may be null: rate 0) and qlog the cells' exchange inflow
+// (may be null: Q 0)
+void launch_cell_summary(const Problem& P, const double* u, const double* g, const double* qlog,
+                         double* out, cudaStream_t s);
+// learned-closure update (coefficients and indicator) and the history push
+void launch_closure_update(const Problem& P, const double* u, const ClosureDev& C, cudaStream_t s);
+void launch_closure_push(const ClosureDev& C, cudaStream_t s);
+// state of a new cell layout: macro part copied, every cell copied or
+// converted (micro -> learned: theta from the summary; learned -> micro:
+// h(theta) on every node)
+void launch_relayout(const Problem& P, int Mn, int Ne, const long long* off_old, const int* learned_old,
+                     const long long* off_new, const int* learned_new, const double* summary,
+                     const double* u_old, double* u_new, cudaStream_t s);
 
 // water content terms, [macro nodes of s | cells of s] scenario by scenario
 // (reduce them with launch_vsum)

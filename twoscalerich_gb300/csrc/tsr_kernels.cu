@@ -26,6 +26,7 @@
 #include "tsr_device.h"
 #include "tsr_internal.h"
 #include "tsr_math.h"
+#include "tsr_mlp.h"
 
 namespace tsr {
 
@@ -122,6 +123,19 @@ __device__ __forceinline__ double vg_se(double h, const VGPar& p, const tsr_math
     double l1 = nL >= 0.0 ? nL + lp : lp;
     double X = tsr_exp(p.mh * l1, T);
     return X * X;
+}
+
+// head at water content theta (inverse retention curve; same operation
+// sequence as the oracle's vg_head): 0 at or above saturation, Se >= 1e-12
+__device__ __forceinline__ double vg_head(double theta, const VGPar& p, const tsr_math_tables* T)
+{
+    double Se = (theta - p.thr) / p.dth;
+    if (!(Se < 1.0)) return 0.0;
+    if (!(Se > 1e-12)) Se = 1e-12;
+    double L = tsr_log(Se, T);
+    double tt = tsr_expm1(-(L / p.m), T);
+    double lt = tsr_log(tt, T);
+    return -(tsr_exp(lt / p.n, T) / p.alpha);
 }
 
 // ---- effective conductivity table --------------------------------------
@@ -335,6 +349,35 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
             }
         }
         __syncthreads();
+        if (D.kind == 1) {
+            // learned closure: one unknown per cell (interior mean water
+            // content), inflow kQ (H_c - h(theta)), rate kT (H_c - h(theta))
+            for (int c = warp; c < nc; c += nwarps) {
+                if (cscen[c] < 0) continue;
+                const int k = ck[c];
+                const double* mc = misc + 16 * c;
+                double Q = 0.0;
+                if (lane == 0) {
+                    const VGPar& pB = S.cell_par ? S.cell_par[k] : P.pB;
+                    const double th = state_at<MODE>(u, v, mc[12], coff[c]);
+                    const double hb = vg_head(th, pB, T);
+                    const double Hc = interp_at(nv, mc, mc[5], mc[6]);
+                    const double d = Hc - hb;
+                    const double g = S.kappa[2 * k + 1] * d;
+                    Q = S.kappa[2 * k] * d;
+                    if (!finite_d(g)) atomicOr(P.flag + cscen[c], 1);
+                    const long long o = coff[c];
+                    if (MODE == 0)
+                        out[o] = g;
+                    else
+                        out[o] = (g - g0[o]) * mc[13];
+                    if (MODE == 0 && P.qlog) P.qlog[k] = Q;
+                }
+                Q = __shfl_sync(0xffffffffu, Q, 0);
+                macro_element_terms(P, k, mc, Q, T, lane);
+            }
+            continue;
+        }
         // nodes: head, conductivity, storage
         for (int idx = tid; idx < nc * mn; idx += bs) {
             const int c = idx / mn, l = idx - c * mn;
@@ -436,6 +479,7 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
                 for (int d = 16; d >= 1; d >>= 1) p = p + __shfl_xor_sync(0xffffffffu, p, d);
                 Q = p;
             }
+            if (MODE == 0 && P.qlog && lane == 0) P.qlog[ck[c]] = Q;
             macro_element_terms(P, ck[c], misc + 16 * c, Q, T, lane);
         }
     }
@@ -868,7 +912,8 @@ __global__ void k_water_cells(Problem P, const double* __restrict__ u, double* _
     const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (k >= M.Ne) return;
     const int nv = M.nv, Ne = M.Ne;
-    const TplDesc D = S.tpl[S.cell_tpl[k]];
+    const bool learned = S.tpl[S.cell_tpl[k]].kind == 1;
+    const TplDesc D = S.tpl[learned ? S.cell_tpl_full[k] : S.cell_tpl[k]];
     const int mn = D.mn;
     const int* bnode = S.bnode + D.node;
     const double* cvm = S.cv + D.node;
@@ -899,6 +944,9 @@ __global__ void k_water_cells(Problem P, const double* __restrict__ u, double* _
                 py = fma(s, vec[mn + l], cy);
             }
             hl = interp_at(nv, al, px, py);
+        } else if (learned) {
+            p = p + u[off] * cvm[l];
+            continue;
         } else {
             hl = u[off + l];
         }
@@ -912,6 +960,236 @@ __global__ void k_water_cells(Problem P, const double* __restrict__ u, double* _
         for (int j = 1; j < nv; ++j) area += M.scv[(long long)j * Ne + k];
         terms[water_slot_cell(M, k)] = (area * M.inv_Y) * ((s * s) * p);
     }
+}
+
+// ---- learned closure ---------------------------------------------------------
+__device__ __forceinline__ double cell_centre_head(const MacroDev& M, const double* u, int k)
+{
+    const int nv = M.nv, Ne = M.Ne;
+    double al[4];
+    for (int m = 0; m < nv; ++m) {
+        long long v0 = M.elements[k];
+        if (M.node_off) v0 = M.node_off[v0];
+        double a = M.sf[(long long)(m * nv) * Ne + k] * u[v0];
+        for (int i = 1; i < nv; ++i) {
+            long long vi = M.elements[(long long)i * Ne + k];
+            if (M.node_off) vi = M.node_off[vi];
+            a = fma(M.sf[(long long)(m * nv + i) * Ne + k], u[vi], a);
+        }
+        al[m] = a;
+    }
+    return interp_at(nv, al, M.cent[k], M.cent[Ne + k]);
+}
+
+// one warp per cell; lane-ordered sums over the interior nodes
+__global__ void k_cell_summary(Problem P, const double* __restrict__ u, const double* __restrict__ g,
+                               const double* __restrict__ qlog, double* __restrict__ out)
+{
+    const MacroDev& M = P.M;
+    const MicroSet& S = P.m;
+    const int lane = threadIdx.x & 31;
+    const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (k >= M.Ne) return;
+    const VGPar& pB = S.cell_par ? S.cell_par[k] : P.pB;
+    const long long off = S.cell_off[k];
+    const TplDesc D = S.tpl[S.cell_tpl[k]];
+    double th, rate;
+    if (D.kind == 1) {
+        th = u[off];
+        rate = g ? g[off] : 0.0;
+    } else {
+        const int mn = D.mn;
+        const int* bnode = S.bnode + D.node;
+        const double* cvm = S.cv + D.node;
+        double pw = 0.0, pt = 0.0, pr = 0.0;
+        for (int l = lane; l < mn; l += 32) {
+            if (bnode[l]) continue;
+            const double h = u[off + l];
+            double K, Cn, Cd;
+            vg_full(h, pB, &d_tables, K, Cn, Cd);
+            const double Se = vg_se(h, pB, &d_tables);
+            const double A = cvm[l];
+            pw = pw + A;
+            pt = pt + fma(pB.dth, Se, pB.thr) * A;
+            if (g) pr = pr + ((Cn / Cd) * g[off + l]) * A;
+        }
+#pragma unroll
+        for (int d = 16; d >= 1; d >>= 1) {
+            pw = pw + __shfl_xor_sync(0xffffffffu, pw, d);
+            pt = pt + __shfl_xor_sync(0xffffffffu, pt, d);
+            pr = pr + __shfl_xor_sync(0xffffffffu, pr, d);
+        }
+        th = pt / pw;
+        rate = g ? pr / pw : 0.0;
+    }
+    if (lane == 0) {
+        double* o = out + 5LL * k;
+        o[0] = cell_centre_head(M, u, k);
+        o[1] = th;
+        o[2] = rate;
+        o[3] = qlog ? qlog[k] : 0.0;
+        o[4] = vg_head(th, pB, &d_tables);
+    }
+}
+
+void launch_cell_summary(const Problem& P, const double* u, const double* g, const double* qlog,
+                         double* out, cudaStream_t s)
+{
+    count();
+    k_cell_summary<<<(P.M.Ne * 32 + 127) / 128, 128, 0, s>>>(P, u, g, qlog, out);
+}
+
+// Features of a learned cell, standardised: log(-H_c), asinh of the head
+// rates over the last 3 accepted steps [m/day], theta, log(-h(theta)).
+__device__ void closure_features(const Problem& P, const ClosureDev& C, const double* u, int k, float z[6],
+                                 int* ood, double* Hc_out, double* hb_out)
+{
+    const MicroSet& S = P.m;
+    const VGPar& pB = S.cell_par ? S.cell_par[k] : P.pB;
+    const double Hc = cell_centre_head(P.M, u, k);
+    const double th = u[S.cell_off[k]];
+    const double hb = vg_head(th, pB, &d_tables);
+    const int nh = C.hcount[k];
+    const double* hs = C.hist + 3LL * k;
+    const double r1 = nh >= 1 ? (Hc - hs[0]) / (C.t[0] - C.t[1]) : 0.0;
+    const double r2 = nh >= 2 ? (hs[0] - hs[1]) / (C.t[1] - C.t[2]) : 0.0;
+    const double r3 = nh >= 3 ? (hs[1] - hs[2]) / (C.t[2] - C.t[3]) : 0.0;
+    double f[6];
+    f[0] = log(fmax(-Hc, 1e-6));
+    f[1] = asinh(r1);
+    f[2] = asinh(r2);
+    f[3] = asinh(r3);
+    f[4] = th;
+    f[5] = log(fmax(-hb, 1e-6));
+    int o = 0;
+    for (int i = 0; i < 6; ++i) {
+        z[i] = (float)((f[i] - C.fmu[i]) / C.fsd[i]);
+        if (!(z[i] >= C.zlo[i] && z[i] <= C.zhi[i])) o = 1;
+    }
+    *ood = o;
+    *Hc_out = Hc;
+    *hb_out = hb;
+}
+
+// one warp per 16 learned cells; network weights staged in shared memory
+__global__ void __launch_bounds__(128) k_closure_update(Problem P, const double* __restrict__ u, ClosureDev C)
+{
+    __shared__ __align__(16) __nv_bfloat16 sw[kMlpParams];
+    __shared__ float feat[4][16][8];
+    __shared__ double hcv[4][16], hbv[4][16];
+    __shared__ int oodv[4][16];
+    const __nv_bfloat16* wg = reinterpret_cast<const __nv_bfloat16*>(C.w);
+    for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) sw[i] = wg[i];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int base = (blockIdx.x * 4 + warp) * 16;
+    if (base >= C.n) return;
+    if (lane < 16) {
+        const int q = base + lane;
+        float z[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        int ood = 0;
+        double Hc = 0.0, hb = 0.0;
+        if (q < C.n) closure_features(P, C, u, C.cells[q], z, &ood, &Hc, &hb);
+        for (int i = 0; i < 6; ++i) feat[warp][lane][i] = z[i];
+        feat[warp][lane][6] = 0.f;
+        feat[warp][lane][7] = 0.f;
+        hcv[warp][lane] = Hc;
+        hbv[warp][lane] = hb;
+        oodv[warp][lane] = ood;
+    }
+    __syncwarp();
+    const int g = lane >> 2, t = lane & 3;
+    float o[4];
+    mlp_forward_warp(feat[warp][g][2 * t], feat[warp][g][2 * t + 1], feat[warp][g + 8][2 * t],
+                     feat[warp][g + 8][2 * t + 1], sw, C.p, o);
+    if (t != 0) return;
+    for (int r = 0; r < 2; ++r) {
+        const int row = g + 8 * r;
+        const int q = base + row;
+        if (q >= C.n) continue;
+        const int k = C.cells[q];
+        const double y1 = (double)o[2 * r] * C.ysd[0] + C.ymu[0];
+        const double y2 = (double)o[2 * r + 1] * C.ysd[1] + C.ymu[1];
+        const double sc = P.cell_scale ? P.cell_scale[k] : 1.0;
+        const double kQ = exp(y1);
+        const double kT = exp(y2) / ((sc * sc) * C.aint[P.m.cell_tpl_full[k]]);
+        const double Hc = hcv[warp][row], hb = hbv[warp][row];
+        const double d = fabs(Hc - hb);
+        int flag = oodv[warp][row];
+        const double kQold = C.kappa[2 * k];
+        if (C.hcount[k] >= 1 && kQold > 0.0) {
+            const double eta = fabs(kQ - kQold) * d / fmax(kQ * d, C.qfloor);
+            if (eta > C.thr) flag = 1;
+        }
+        C.kappa[2 * k] = kQ;
+        C.kappa[2 * k + 1] = kT;
+        C.hcur[k] = Hc;
+        C.flags[k] = flag;
+        if (flag) atomicAdd(C.nflag, 1);
+    }
+}
+
+void launch_closure_update(const Problem& P, const double* u, const ClosureDev& C, cudaStream_t s)
+{
+    if (C.n <= 0) return;
+    count();
+    k_closure_update<<<(C.n + 63) / 64, 128, 0, s>>>(P, u, C);
+}
+
+__global__ void k_closure_push(ClosureDev C)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= C.n) return;
+    const int k = C.cells[q];
+    double* h = C.hist + 3LL * k;
+    h[2] = h[1];
+    h[1] = h[0];
+    h[0] = C.hcur[k];
+    if (C.hcount[k] < 3) C.hcount[k] += 1;
+}
+
+void launch_closure_push(const ClosureDev& C, cudaStream_t s)
+{
+    if (C.n <= 0) return;
+    count();
+    k_closure_push<<<(C.n + 127) / 128, 128, 0, s>>>(C);
+}
+
+// macro part by a strided loop of block 0..; cells one warp each
+__global__ void k_relayout(Problem P, int Mn, int Ne, const long long* __restrict__ off_old,
+                           const int* __restrict__ learned_old, const long long* __restrict__ off_new,
+                           const int* __restrict__ learned_new, const double* __restrict__ summary,
+                           const double* __restrict__ u_old, double* __restrict__ u_new)
+{
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nthr = gridDim.x * blockDim.x;
+    for (int i = gt; i < Mn; i += nthr) u_new[i] = u_old[i];
+    const int lane = threadIdx.x & 31;
+    const int k = gt >> 5;
+    if (k >= Ne) return;
+    const MicroSet& S = P.m;
+    const int mn = S.tpl[S.cell_tpl_full[k]].mn;
+    const long long a = off_old[k], b = off_new[k];
+    const int lo = learned_old[k], ln = learned_new[k];
+    if (lo == ln) {
+        const int n = lo ? 1 : mn;
+        for (int l = lane; l < n; l += 32) u_new[b + l] = u_old[a + l];
+    } else if (ln) {
+        if (lane == 0) u_new[b] = summary[5LL * k + 1];
+    } else {
+        const VGPar& pB = S.cell_par ? S.cell_par[k] : P.pB;
+        const double hb = vg_head(u_old[a], pB, &d_tables);
+        for (int l = lane; l < mn; l += 32) u_new[b + l] = hb;
+    }
+}
+
+void launch_relayout(const Problem& P, int Mn, int Ne, const long long* off_old, const int* learned_old,
+                     const long long* off_new, const int* learned_new, const double* summary,
+                     const double* u_old, double* u_new, cudaStream_t s)
+{
+    count();
+    k_relayout<<<(Ne * 32 + 127) / 128, 128, 0, s>>>(P, Mn, Ne, off_old, learned_old, off_new, learned_new,
+                                                      summary, u_old, u_new);
 }
 
 void launch_water_terms(const Problem& P, const double* u, double* terms, cudaStream_t s)

@@ -170,6 +170,26 @@ class Problem:
         self.tspan = np.array([0.0])
         self.tend = 1.0
 
+    def set_learned(self, learned, kappa=None):
+        """Learned-closure layout (one scenario): cell k with learned[k]
+        carries one unknown instead of its micro nodes; kappa (2 Ne) are the
+        closure coefficients (kQ, kT) per cell.  Contexts built afterwards
+        can switch cells at run time (tsr_closure_set_learned)."""
+        assert self.S == 1
+        if not hasattr(self, "cell_nodes_full"):
+            self.cell_nodes_full = self.cell_nodes.copy()
+            self.N_full = self.N
+        self._learned = np.ascontiguousarray(learned, dtype=np.int32)
+        self._kappa = (np.zeros(2 * self.Ne) if kappa is None
+                       else np.ascontiguousarray(kappa, dtype=np.float64))
+        self.ext.cell_learned = ptr(self._learned)
+        self.ext.closure_coef = ptr(self._kappa)
+        self.cell_nodes = np.where(self._learned != 0, 1, self.cell_nodes_full).astype(np.int64)
+        self.cell_off = self.Mn + np.concatenate([[0], np.cumsum(self.cell_nodes)[:-1]]).astype(np.int64)
+        self.N = int(self.Mn + self.cell_nodes.sum())
+        self.scen_start = np.array([0, self.N], dtype=np.int64)
+        self.ud.N = self.N
+
     def initial_state(self, h0=-5.0, noise=0.0, seed=EVAL_SEED):
         """h0 (a number, or one number per scenario) plus optional noise;
         Dirichlet nodes at their head."""
