@@ -492,15 +492,17 @@ def run_ensemble(args):
             for s in range(S):
                 if done_at[s] is None and (t[s] >= p.tend or status[s] != 0):
                     done_at[s] = now
-            if nrun == 0:
+            if nrun == 0 or now > args.to_end_seconds:
                 break
-        wall = sorted(done_at)
-        to_end = {"rounds": rounds, "wall_s_total": wall[-1],
-                  "p50_scenario_wall_s": float(np.percentile(wall, 50)),
-                  "p95_scenario_wall_s": float(np.percentile(wall, 95)),
+        fin = sorted(x for x in done_at if x is not None)
+        to_end = {"rounds": rounds, "wall_s": now, "finished": len(fin), "scenarios": S,
+                  "stopped_by_time_cap": nrun > 0,
+                  "p50_scenario_wall_s": float(np.percentile(fin, 50)) if len(fin) == S else None,
+                  "p95_scenario_wall_s": float(np.percentile(fin, 95)) if len(fin) == S else None,
+                  "t_reached_p5_p50_p95": [float(np.percentile(t, q)) for q in (5, 50, 95)],
                   "steps_per_scenario": [st2[s].NumSteps for s in range(S)],
                   "failed": int(sum(1 for s in range(S) if status[s] != 0)),
-                  "scenario_steps_per_s": sum(st2[s].NumSteps for s in range(S)) / wall[-1]}
+                  "scenario_steps_per_s": sum(st2[s].NumSteps for s in range(S)) / now}
     cpu = None
     if RANK == 0 and WORLD == 1 and not args.no_cpu_baseline:
         cpu = cpu_ensemble_rate(p, args.cpu_seconds)
@@ -533,6 +535,73 @@ def run_ensemble(args):
         dist.destroy_process_group()
 
 
+def run_closure_bench(args):
+    """Config 5: the learned closure against the plain FP64 method on the
+    same 301 x 301 / 21 x 21 mesh.  The network is trained on the GPU from
+    plain-run data (configurations 1 and 2, seeds 1001-1002); both runs go
+    from t = 0 to the same output times; value = plain wall time / closure
+    wall time (higher is better)."""
+    from twoscalerich_gb300 import closure
+    from twoscalerich_gb300 import problem as P
+    if RANK != 0:
+        return
+    t_all = time.perf_counter()
+    msgs = []
+    X, Y, desc = closure.training_set(time_limit=args.log_seconds, log=lambda m: msgs.append(m))
+    t_data = time.perf_counter() - t_all
+    t0 = time.perf_counter()
+    model, hist, err = closure.train_model(X, Y, epochs=args.epochs, batch=4096, lr=2e-3, seed=1001)
+    t_train = time.perf_counter() - t0
+    times = [float(x) for x in args.times.split(",")]
+    mk = lambda: P.config2(n_macro=args.n_macro, n_micro=args.n_micro)
+    rp, wp, sp, fp = closure.run_plain(mk(), times)
+    # indicator: change of a cell's inflow over a step relative to the
+    # largest inflow of the field at t = 0 (norm-wise relative flux error)
+    from twoscalerich_gb300.capi import TsrError
+
+    def attempt(**kw):
+        try:
+            return closure.run_closure(mk(), model, times, thr=args.indicator, qfloor_rel=1.0, **kw), None
+        except TsrError as e:
+            return None, str(e)
+    res, fail_c = attempt()
+    flagged = list(getattr(closure.run_closure, "flagged_per_step", []))
+    if res is None:
+        print(json.dumps({"metric": "learned-closure speed-up", "value": None, "error": fail_c}))
+        return
+    rc, wc, sc, fc, frac = res
+    resu, fail_u = attempt(params=closure.init_params(7), max_steps=600)
+    ru, wu, su, fu, fracu = resu if resu is not None else ([], None, None, None, None)
+
+    def errs(rec):
+        return [{"t": a[0], "water_rel": abs(a[1] - b[1]) / abs(b[1]),
+                 "h_max_abs": float(np.max(np.abs(a[2] - b[2]))),
+                 "h_rel": float(np.max(np.abs(a[2] - b[2])) / np.max(np.abs(b[2])))}
+                for a, b in zip(rec, rp)]
+    line = {
+        "metric": "learned-closure speed-up over the plain FP64 GPU run (wall time to the last output time)",
+        "value": wp / wc, "unit": "x", "n_gpus": 1, "steps": sc, "warmup": 0,
+        "ms_per_step": 1e3 * wc / max(sc, 1), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 state, bf16 network", "data": "synthetic",
+        "config": {"workload": "learned closure, two-scale Richards", "indicator_kind":
+                   "|dkQ| |H_c - h| <= thr * max|Q(t=0)| per step", "macro_nodes":
+                   "%dx%d" % (args.n_macro, args.n_macro), "micro_nodes_per_cell":
+                   "%dx%d" % (args.n_micro, args.n_micro), "cells": 2 * (args.n_macro - 1) ** 2,
+                   "output_times_d": times, "indicator": args.indicator,
+                   "network": "6 -> 4 x 64 SiLU -> 2, bf16 mma.sync, fp32 accumulation"},
+        "plain": {"wall_s": wp, "steps": sp, "g_evals": fp, "water": [r[1] for r in rp]},
+        "closure": {"wall_s": wc, "steps": sc, "g_evals": fc, "fallback_fraction": frac,
+                    "errors": errs(rc), "out_of_range_at_t0": getattr(closure.run_closure, "ood_t0", None),
+                    "flagged_per_step_first": flagged[:12], "flagged_total": int(sum(flagged))},
+        "ablation_untrained": {"wall_s": wu, "steps": su, "fallback_fraction": fracu, "errors": errs(ru),
+                               "note": "untrained network (seed 7), at most 600 steps", "error": fail_u},
+        "training": {"samples": int(X.shape[0]), "data_s": t_data, "train_s": t_train,
+                     "epochs": args.epochs, "loss": [float(x) for x in hist], "heldout": err,
+                     "runs": desc},
+    }
+    print(json.dumps(line))
+
+
 # FP64 instructions (DADD + DMUL + DFMA, thread level) per unknown of one
 # finite-difference Jv launch of the cell kernel, and its DRAM bytes (read +
 # write) per unknown, from the ncu capture of the 141x141 / 21x21 case in
@@ -553,16 +622,24 @@ def main():
     ap.add_argument("--cpu-evals", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--max-krylov", type=int, default=None)
-    ap.add_argument("--config", type=int, default=2, choices=[2, 3, 4],
+    ap.add_argument("--config", type=int, default=2, choices=[2, 3, 4, 5],
                     help="2: 201x201 x 21x21 plain method; 3: 151x151 batched uneven cells; "
-                         "4: 64-scenario ensemble of 51x51 x 15x15")
+                         "4: 64-scenario ensemble of 51x51 x 15x15; 5: learned closure, 301x301")
+    ap.add_argument("--times", default="1e-4,2.5e-4,5e-4", help="config 5 output times [d]")
+    ap.add_argument("--indicator", type=float, default=1e-3)
+    ap.add_argument("--epochs", type=int, default=8)
+    ap.add_argument("--log-seconds", type=float, default=45.0)
     ap.add_argument("--scenarios", type=int, default=64)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--to-end", action="store_true",
                     help="config 4: also run every scenario to t_end (p50/p95 wall time)")
+    ap.add_argument("--to-end-seconds", type=float, default=600.0,
+                    help="config 4: wall-time cap of the run to t_end")
     args = ap.parse_args()
     if args.config == 3 and args.n_macro == 201:
         args.n_macro = 151
+    if args.config == 5 and args.n_macro == 201:
+        args.n_macro = 301
     if args.config == 4:
         if args.n_macro == 201:
             args.n_macro = 51
@@ -574,6 +651,8 @@ def main():
         run_reference(args)
     elif args.config == 4:
         run_ensemble(args)
+    elif args.config == 5:
+        run_closure_bench(args)
     else:
         run_ours(args)
 

@@ -20,7 +20,8 @@ Jacobian of EXPREM sees the exact linearisation of the closure.
 
 After every step an a-posteriori indicator compares the inflow the held
 coefficients gave with the one the network gives at the new state,
-|kQ' - kQ| |H_c - h| / max(kQ' |H_c - h|, q_floor), and flags inputs outside
+|kQ' - kQ| |H_c - h| / max(kQ' |H_c - h|, q_floor) (from a cell's second
+learned step on), and flags inputs outside
 the training range; flagged cells fall back to their micro meshes and the
 plain FP64 cell kernel for the rest of the run.
 
@@ -99,11 +100,12 @@ def log_plain_run(p, max_steps=100000, cell_stride=1, time_limit=None):
     return logs
 
 
-def samples(p, logs, cell_stride=1, min_gap=1e-9):
-    """(X [n, 8] float32 with 6 inputs, Y [n, 2] float32 targets) from a log."""
+def samples(p, logs, cell_stride=1, min_gap=1e-9, skip=0):
+    """(X [n, 8] float32 with 6 inputs, Y [n, 2] float32 targets) from a
+    log, leaving out the first `skip` steps."""
     aint = interior_area(p)[::cell_stride]
     Xs, Ys = [], []
-    for n in range(1, len(logs)):
+    for n in range(max(1, skip), len(logs)):
         t = [logs[n - i][0] if n - i >= 0 else np.nan for i in range(4)]
         S = logs[n][1].astype(np.float64)
         Hc, th, rate, Q, hb = S[:, 0], S[:, 1], S[:, 2], S[:, 3], S[:, 4]
@@ -315,10 +317,16 @@ def run_closure(p, model, times, thr=1e-3, qfloor_rel=1e-3, auto_fallback=True, 
     summ = np.empty(5 * p.Ne)
     check(lib.tsr_cell_summary(ctx.h, None, ptr(summ)), "summary")
     q0 = float(np.max(np.abs(summ.reshape(-1, 5)[:, 3])))
-    check(lib.tsr_closure_set_learned(ctx.h, np.ones(p.Ne, dtype=np.int32).ctypes.data_as(capi.ip)),
-          "set_learned")
-    check(lib.tsr_closure_attach(ctx.h, net.h, ptr(model.norm()), model.zrange().ctypes.data_as(capi.fp),
+    ones = np.ones(p.Ne, dtype=np.int32)
+    check(lib.tsr_closure_set_learned(ctx.h, ones.ctypes.data_as(capi.ip)), "set_learned")
+    norm, zr = model.norm(), model.zrange()      # alive for the duration of the calls
+    check(lib.tsr_closure_attach(ctx.h, net.h, ptr(norm), zr.ctypes.data_as(capi.fp),
                                  thr, qfloor_rel * q0, int(auto_fallback)), "attach")
+    # inputs of the network at t = 0 against the accepted range (diagnostic)
+    S0 = summ.reshape(-1, 5)
+    f0 = features(S0[:, 0], np.full((p.Ne, 3), np.nan), [0.0, -1e30, -1e30, -1e30], S0[:, 1], S0[:, 4])
+    z0 = (f0 - model.fmu) / model.fsd
+    ood0 = [float(np.mean((z0[:, i] < model.zlo[i]) | (z0[:, i] > model.zhi[i]))) for i in range(N_FEAT)]
     st = capi.ExpremStats()
     t = C.c_double(0.0)
     nf = C.c_int()
@@ -328,10 +336,12 @@ def run_closure(p, model, times, thr=1e-3, qfloor_rel=1e-3, auto_fallback=True, 
     check(lib.tsr_sync(ctx.h), "sync")
     w0 = time.perf_counter()
     wall = 0.0
+    nfl = []
     for tk in times:
         while t.value < tk and st.NumSteps < max_steps:
             check(lib.tsr_closure_advance(ctx.h, tk, ptr(tspan), None, C.byref(p.options), C.byref(st),
                                           C.byref(t), C.byref(nf)), "closure_advance")
+            nfl.append(nf.value)
         check(lib.tsr_sync(ctx.h), "sync")
         wall += time.perf_counter() - w0
         n = lib.tsr_num_unknowns(ctx.h)
@@ -345,4 +355,36 @@ def run_closure(p, model, times, thr=1e-3, qfloor_rel=1e-3, auto_fallback=True, 
         w0 = time.perf_counter()
     ctx.close()
     net.close()
+    run_closure.ood_t0 = ood0
+    run_closure.flagged_per_step = nfl
     return rec, wall, st.NumSteps, st.FuncEvals, frac
+
+
+def training_set(time_limit=45.0, skip=3, log=print):
+    """Training data from plain runs of the CPU-runnable configuration (two
+    initial heads drawn from seeds 1001-1002) and of the GPU-scale plain
+    configuration at 101 x 101 macro nodes (inclusion sizes and initial
+    noise from seeds 1001-1002), each run for at most time_limit seconds;
+    the first `skip` steps of every run (the decay of the initial noise)
+    are left out.  Returns (X, Y, description)."""
+    X, Y, desc = [], [], []
+    for seed in (1001, 1002):
+        q = P.config1()
+        h0 = float(np.random.default_rng(seed).uniform(-8.0, -2.0))
+        q.u0 = q.initial_state(h0)
+        logs = log_plain_run(q, time_limit=time_limit)
+        x, y = samples(q, logs, skip=skip)
+        X.append(x)
+        Y.append(y)
+        desc.append("21x21/11x11 h0=%.2f: %d steps to t=%.3g d, %d samples" % (h0, len(logs) - 1, logs[-1][0], len(x)))
+        log(desc[-1])
+    for seed in (1001, 1002):
+        q = P.config2(n_macro=101, seed=seed, eval_seed=seed + 1000)
+        logs = log_plain_run(q, cell_stride=2, time_limit=time_limit)
+        x, y = samples(q, logs, cell_stride=2, skip=skip)
+        X.append(x)
+        Y.append(y)
+        desc.append("101x101/21x21 seed %d: %d steps to t=%.3g d, %d samples (every 2nd cell)"
+                    % (seed, len(logs) - 1, logs[-1][0], len(x)))
+        log(desc[-1])
+    return np.concatenate(X), np.concatenate(Y), desc
