@@ -535,6 +535,56 @@ def run_ensemble(args):
         dist.destroy_process_group()
 
 
+def run_to_end_bench(args):
+    """Config 1 (21 x 21 macro, 11 x 11 micro, t_end = 1 d): wall seconds
+    from t = 0 to t_end through the reference-facing one-step call, on the
+    GPU (tsr_exprem_step, u in pinned host memory) and on the host cores
+    (the oracle's OpenMP EXPREM with C-library log/exp)."""
+    import oracle
+    from twoscalerich_gb300 import capi
+    from twoscalerich_gb300 import problem as P
+    if RANK != 0:
+        return
+    p = P.config1()
+    ctx = P.Context(p)
+    for _ in range(args.warmup):                      # warm: one full run
+        P.run_to_end(ctx.exprem_step, p)
+    clocks = Clocks()
+    clocks.start()
+    l0 = ctx.lib.tsr_kernel_launches()
+    t0 = time.perf_counter()
+    runs = []
+    for _ in range(args.steps):
+        r0 = time.perf_counter()
+        u, solns, st, log = P.run_to_end(ctx.exprem_step, p)
+        runs.append(time.perf_counter() - r0)
+    launches = ctx.lib.tsr_kernel_launches() - l0
+    clk = clocks.stop()
+    gpu_s = float(np.median(runs))
+    threads = os.cpu_count() or 1
+    orc = oracle.Oracle(p, nthreads=threads, libm=True)
+    c0 = time.perf_counter()
+    uc, sc, stc, logc = P.run_to_end(orc.exprem_step, p)
+    cpu_s = time.perf_counter() - c0
+    line = {
+        "metric": "wall seconds to t_end (config 1, EXPREM through the one-step call)",
+        "value": gpu_s, "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * gpu_s / max(st.NumSteps, 1), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "two-scale Richards, 21x21 macro, 11x11 micro, t_end = 1 d",
+                   "unknowns": p.N, "accepted_steps": st.NumSteps, "g_evals": st.FuncEvals,
+                   "inputs_vs_l2": "working set 0.4 GB of vectors and basis; repeated runs"},
+        "runs_s": runs,
+        "cpu_baseline": {"value": cpu_s, "unit": "s", "cores": threads, "kind": "port",
+                         "sample": "one full run to t_end (%d steps) by the oracle's OpenMP EXPREM "
+                                   "with C-library log/exp" % stc.NumSteps},
+        "speedup_vs_cpu": cpu_s / gpu_s,
+        "e2e": {"value": gpu_s, "unit": "s", "h2d_bytes_per_step": 8 * p.N, "d2h_bytes_per_step": 8 * p.N},
+        "clocks": clk, "gpu_launches": int(launches),
+    }
+    print(json.dumps(line))
+
+
 def run_closure_bench(args):
     """Config 5: the learned closure against the plain FP64 method on the
     same 301 x 301 / 21 x 21 mesh.  The network is trained on the GPU from
@@ -622,8 +672,9 @@ def main():
     ap.add_argument("--cpu-evals", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--max-krylov", type=int, default=None)
-    ap.add_argument("--config", type=int, default=2, choices=[2, 3, 4, 5],
-                    help="2: 201x201 x 21x21 plain method; 3: 151x151 batched uneven cells; "
+    ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4, 5],
+                    help="1: 21x21 x 11x11 to t_end; 2: 201x201 x 21x21 plain method; "
+                         "3: 151x151 batched uneven cells; "
                          "4: 64-scenario ensemble of 51x51 x 15x15; 5: learned closure, 301x301")
     ap.add_argument("--times", default="1e-4,2.5e-4,5e-4", help="config 5 output times [d]")
     ap.add_argument("--indicator", type=float, default=1e-3)
@@ -653,6 +704,8 @@ def main():
         run_ensemble(args)
     elif args.config == 5:
         run_closure_bench(args)
+    elif args.config == 1:
+        run_to_end_bench(args)
     else:
         run_ours(args)
 

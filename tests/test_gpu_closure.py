@@ -49,6 +49,23 @@ def test_mlp_fused_equals_layered_and_oracle():
     net.close()
 
 
+def test_mlp_tcgen05_matches_mma_sync_and_oracle():
+    """the tcgen05 / tensor-memory inference (one CTA per 128 rows) against
+    the mma.sync kernel and the oracle; the two tensor-core paths may
+    accumulate in a different order, so agreement is to BF16 resolution"""
+    params = om.init_params(13)
+    net = closure.Mlp(params)
+    x = _x(1000, 6)
+    yt = net.forward(x, fused="tcgen05")
+    ym = net.forward(x, fused=True)
+    yo, _ = om.forward(params, x, bf=True)
+    scale = np.max(np.abs(yo))
+    assert np.max(np.abs(yt - ym)) / scale < 2e-3
+    d = np.abs(yt - yo) / scale
+    assert np.max(d) < 2e-3 and np.median(d) < 1e-5, (np.max(d), np.median(d))
+    net.close()
+
+
 def test_mlp_gradient_matches_oracle():
     params = om.init_params(12)
     net = closure.Mlp(params)
@@ -76,6 +93,44 @@ def test_mlp_training_lowers_loss():
     hist = net.train(x, y, epochs=6, batch=1024, lr=3e-3, seed=1001)
     l1 = float(np.mean((net.forward(x) - y) ** 2))
     assert hist[-1] < hist[0] and l1 < 0.2 * l0, (hist, l0, l1)
+    net.close()
+
+
+def test_closure_update_matches_oracle_network():
+    """the per-step coefficients of the learned cells (features in FP64,
+    network on tcgen05) against the oracle network on the same features"""
+    p = P.config1()
+    p.set_learned(np.zeros(p.Ne, dtype=np.int32))
+    ctx = P.Context(p)
+    lib = ctx.lib
+    u = p.u0 + np.random.default_rng(5).uniform(-0.5, 0.5, p.N)
+    capi.check(lib.tsr_exprem_load(ctx.h, capi.ptr(u), 0.0), "load")
+    summ = np.empty(5 * p.Ne)
+    capi.check(lib.tsr_cell_summary(ctx.h, None, capi.ptr(summ)), "summary")
+    S = summ.reshape(p.Ne, 5)
+    capi.check(lib.tsr_closure_set_learned(ctx.h, np.ones(p.Ne, dtype=np.int32).ctypes.data_as(capi.ip)),
+               "relayout")
+    f = closure.features(S[:, 0], np.full((p.Ne, 3), np.nan), [0.0, -1e30, -1e30, -1e30], S[:, 1], S[:, 4])
+    fmu, fsd = f.mean(0), f.std(0) + 1e-3
+    norm = np.concatenate([fmu, fsd, [-8.0, -8.0], [1.5, 1.5]])
+    zr = np.concatenate([np.full(6, -1e3), np.full(6, 1e3)]).astype(np.float32)
+    params = om.init_params(21)
+    net = closure.Mlp(params)
+    capi.check(lib.tsr_closure_attach(ctx.h, net.h, capi.ptr(norm), zr.ctypes.data_as(capi.fp), 1e-3, 0.0, 0),
+               "attach")
+    nf = C.c_int()
+    capi.check(lib.tsr_closure_update(ctx.h, C.byref(nf)), "update")
+    assert nf.value == 0
+    kappa = np.empty(2 * p.Ne)
+    capi.check(lib.tsr_closure_read(ctx.h, None, capi.ptr(kappa), None), "read")
+    x = np.zeros((p.Ne, 8), dtype=np.float32)
+    x[:, :6] = ((f - fmu) / fsd).astype(np.float32)
+    yo, _ = om.forward(params, x, bf=True)
+    lq = yo[:, 0] * 1.5 - 8.0
+    lt = yo[:, 1] * 1.5 - 8.0 - np.log(closure.interior_area(p))
+    tol = 1.5 * 2e-3 * np.max(np.abs(yo))
+    assert np.max(np.abs(np.log(kappa[0::2]) - lq)) <= tol
+    assert np.max(np.abs(np.log(kappa[1::2]) - lt)) <= tol
     net.close()
 
 

@@ -195,6 +195,10 @@ class Mlp:
         return p
 
     def forward(self, x, fused=True):
+        """fused: True (mma.sync, activations in registers), False (the
+        layer-by-layer training path) or "tcgen05" (tensor memory)."""
+        if fused == "tcgen05":
+            fused = 2
         x = np.ascontiguousarray(x, dtype=np.float32)
         y = np.empty((x.shape[0], 2), dtype=np.float32)
         check(self.lib.tsr_mlp_forward(self.h, x.ctypes.data_as(capi.fp), x.shape[0],

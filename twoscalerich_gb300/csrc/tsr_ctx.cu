@@ -1953,15 +1953,19 @@ extern "C" int tsr_closure_attach(tsr_ctx* c, tsr_mlp* mlp, const double* norm, 
 extern "C" int tsr_closure_update(tsr_ctx* c, int* n_flagged)
 {
     if (!c || !c->closure || !c->mlp || !c->sc[0].loaded) return TSR_ERR_ARG;
-    CK(cudaMemsetAsync(c->d_nflag, 0, sizeof(int), c->stream));
+    // word 0: flagged cells; word 1: a bounded wait of the network expired
+    CK(cudaMemsetAsync(c->d_nflag, 0, 2 * sizeof(int), c->stream));
     ClosureDev C = closure_dev(c);
     launch_closure_update(c->P, c->d_u, C, c->stream);
     CK(cudaGetLastError());
-    int nf = 0;
-    CK(cudaMemcpyAsync(c->h_flag, c->d_nflag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    nf = c->h_flag[0];
-    if (n_flagged) *n_flagged = nf;
+    int w[2] = {0, 0};
+    CK(cudaMemcpy(w, c->d_nflag, 2 * sizeof(int), cudaMemcpyDeviceToHost));
+    if (w[1]) {
+        set_error("closure update: a wait on the tensor-core barrier expired");
+        return TSR_ERR_TIMEOUT;
+    }
+    if (n_flagged) *n_flagged = w[0];
     return TSR_OK;
 }
 

@@ -27,6 +27,7 @@
 #include "tsr_internal.h"
 #include "tsr_math.h"
 #include "tsr_mlp.h"
+#include "tsr_mlp_tc.cuh"
 
 namespace tsr {
 
@@ -1071,51 +1072,36 @@ __device__ void closure_features(const Problem& P, const ClosureDev& C, const do
     *hb_out = hb;
 }
 
-// one warp per 16 learned cells; network weights staged in shared memory
+// one CTA per 128 learned cells (one thread per cell), the network on
+// tcgen05 with its accumulators in tensor memory (tsr_mlp_tc.cuh)
 __global__ void __launch_bounds__(128) k_closure_update(Problem P, const double* __restrict__ u, ClosureDev C)
 {
-    __shared__ __align__(16) __nv_bfloat16 sw[kMlpParams];
-    __shared__ float feat[4][16][8];
-    __shared__ double hcv[4][16], hbv[4][16];
-    __shared__ int oodv[4][16];
-    const __nv_bfloat16* wg = reinterpret_cast<const __nv_bfloat16*>(C.w);
-    for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) sw[i] = wg[i];
+    extern __shared__ __align__(1024) unsigned char tcsm[];
+    uint32_t* slot = reinterpret_cast<uint32_t*>(tcsm + kTcBar + 8);
+    tc_stage_weights(reinterpret_cast<const __nv_bfloat16*>(C.w), tcsm);
+    tc_bar_init(tcsm);
+    tc_alloc(slot);
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int base = (blockIdx.x * 4 + warp) * 16;
-    if (base >= C.n) return;
-    if (lane < 16) {
-        const int q = base + lane;
-        float z[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        int ood = 0;
-        double Hc = 0.0, hb = 0.0;
-        if (q < C.n) closure_features(P, C, u, C.cells[q], z, &ood, &Hc, &hb);
-        for (int i = 0; i < 6; ++i) feat[warp][lane][i] = z[i];
-        feat[warp][lane][6] = 0.f;
-        feat[warp][lane][7] = 0.f;
-        hcv[warp][lane] = Hc;
-        hbv[warp][lane] = hb;
-        oodv[warp][lane] = ood;
-    }
-    __syncwarp();
-    const int g = lane >> 2, t = lane & 3;
-    float o[4];
-    mlp_forward_warp(feat[warp][g][2 * t], feat[warp][g][2 * t + 1], feat[warp][g + 8][2 * t],
-                     feat[warp][g + 8][2 * t + 1], sw, C.p, o);
-    if (t != 0) return;
-    for (int r = 0; r < 2; ++r) {
-        const int row = g + 8 * r;
-        const int q = base + row;
-        if (q >= C.n) continue;
-        const int k = C.cells[q];
-        const double y1 = (double)o[2 * r] * C.ysd[0] + C.ymu[0];
-        const double y2 = (double)o[2 * r + 1] * C.ysd[1] + C.ymu[1];
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *slot;
+    const int q = blockIdx.x * kTcRows + threadIdx.x;
+    const bool mine = q < C.n;
+    const int k = mine ? C.cells[q] : 0;
+    float z[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    int ood = 0;
+    double Hc = 0.0, hb = 0.0;
+    if (mine) closure_features(P, C, u, k, z, &ood, &Hc, &hb);
+    auto x_at = [&](int, int c) -> float { return z[c]; };
+    auto out = [&](int, float o1, float o2) {
+        if (!mine) return;
+        const double y1 = (double)o1 * C.ysd[0] + C.ymu[0];
+        const double y2 = (double)o2 * C.ysd[1] + C.ymu[1];
         const double sc = P.cell_scale ? P.cell_scale[k] : 1.0;
         const double kQ = exp(y1);
         const double kT = exp(y2) / ((sc * sc) * C.aint[P.m.cell_tpl_full[k]]);
-        const double Hc = hcv[warp][row], hb = hbv[warp][row];
         const double d = fabs(Hc - hb);
-        int flag = oodv[warp][row];
+        int flag = ood;
         const double kQold = C.kappa[2 * k];
         // the change of kQ over the last step (from the second step of the
         // cell on: its first step had no coefficients of its own yet)
@@ -1128,14 +1114,18 @@ __global__ void __launch_bounds__(128) k_closure_update(Problem P, const double*
         C.hcur[k] = Hc;
         C.flags[k] = flag;
         if (flag) atomicAdd(C.nflag, 1);
-    }
+    };
+    uint32_t phase = 0;
+    tc_forward_tile(tcsm, tmem, C.p, x_at, out, phase, C.nflag + 1);
+    __syncthreads();
+    tc_free(tmem);
 }
 
 void launch_closure_update(const Problem& P, const double* u, const ClosureDev& C, cudaStream_t s)
 {
     if (C.n <= 0) return;
     count();
-    k_closure_update<<<(C.n + 63) / 64, 128, 0, s>>>(P, u, C);
+    k_closure_update<<<(C.n + kTcRows - 1) / kTcRows, kTcRows, kTcSmem, s>>>(P, u, C);
 }
 
 __global__ void k_closure_push(ClosureDev C)

@@ -24,6 +24,7 @@
 #include "../../include/tsr_capi.h"
 #include "tsr_internal.h"
 #include "tsr_mlp.h"
+#include "tsr_mlp_tc.cuh"
 
 using namespace tsr;
 
@@ -314,6 +315,37 @@ __global__ void __launch_bounds__(128) k_mlp_infer(const float* __restrict__ x, 
     }
 }
 
+// fused inference on tcgen05 (tsr_mlp_tc.cuh): one CTA per 128 rows
+__global__ void __launch_bounds__(128) k_mlp_infer_tc(const float* __restrict__ x, int rows,
+                                                      const __nv_bfloat16* __restrict__ w,
+                                                      const float* __restrict__ p, float* __restrict__ y,
+                                                      int* __restrict__ err)
+{
+    extern __shared__ __align__(1024) unsigned char sm[];
+    uint32_t* slot = reinterpret_cast<uint32_t*>(sm + kTcBar + 8);
+    tc_stage_weights(w, sm);
+    tc_bar_init(sm);
+    tc_alloc(slot);
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *slot;
+    uint32_t phase = 0;
+    const int r0 = blockIdx.x * kTcRows;
+    auto x_at = [&](int r, int c) -> float {
+        return (r0 + r < rows) ? x[(long long)(r0 + r) * kRowStride + c] : 0.0f;
+    };
+    auto out = [&](int r, float a, float b) {
+        if (r0 + r < rows) {
+            y[(long long)(r0 + r) * kMlpOut] = a;
+            y[(long long)(r0 + r) * kMlpOut + 1] = b;
+        }
+    };
+    tc_forward_tile(sm, tmem, p, x_at, out, phase, err);
+    __syncthreads();
+    tc_free(tmem);
+}
+
 }  // namespace
 
 struct tsr_mlp {
@@ -329,6 +361,7 @@ struct tsr_mlp {
     float *z[5] = {}, *a[5] = {}, *dz = nullptr, *da = nullptr, *dx = nullptr;
     int step = 0;
     cudaStream_t s = nullptr;
+    int* d_err = nullptr;
 };
 
 namespace {
@@ -439,7 +472,8 @@ extern "C" tsr_mlp* tsr_mlp_create(void)
          cudaMalloc(&m->d_m, pb) == cudaSuccess && cudaMalloc(&m->d_v, pb) == cudaSuccess &&
          cudaMalloc(&m->d_decay, kMlpParams) == cudaSuccess &&
          cudaMalloc(&m->d_w, sizeof(__nv_bfloat16) * kMlpParams) == cudaSuccess &&
-         cudaMalloc(&m->d_wt, sizeof(__nv_bfloat16) * kMlpParams) == cudaSuccess;
+         cudaMalloc(&m->d_wt, sizeof(__nv_bfloat16) * kMlpParams) == cudaSuccess &&
+         cudaMalloc(&m->d_err, sizeof(int)) == cudaSuccess && cudaMemset(m->d_err, 0, sizeof(int)) == cudaSuccess;
     if (ok) {
         std::vector<unsigned char> dec(kMlpParams, 0);
         const int wo[5] = {kW1, kW2, kW3, kW4, kW5};
@@ -465,7 +499,7 @@ extern "C" void tsr_mlp_free(tsr_mlp* m)
     if (!m) return;
     if (m->s) cudaStreamSynchronize(m->s);
     mlp_free_batch(m);
-    void* ps[] = {m->d_p, m->d_g, m->d_m, m->d_v, m->d_decay, m->d_w, m->d_wt, m->d_x, m->d_y, m->d_idx};
+    void* ps[] = {m->d_p, m->d_g, m->d_m, m->d_v, m->d_decay, m->d_w, m->d_wt, m->d_x, m->d_y, m->d_idx, m->d_err};
     for (void* p : ps)
         if (p) cudaFree(p);
     if (m->s) cudaStreamDestroy(m->s);
@@ -507,6 +541,21 @@ extern "C" int tsr_mlp_forward(tsr_mlp* m, const float* x_host, int n, float* y_
     int rc = mlp_reserve(m, n);
     if (rc) return rc;
     CKM(cudaMemcpyAsync(m->b_x, x_host, sizeof(float) * (size_t)n * kRowStride, cudaMemcpyHostToDevice, m->s));
+    if (fused == 2) {
+        CKM(cudaMemsetAsync(m->d_err, 0, sizeof(int), m->s));
+        k_mlp_infer_tc<<<(n + kTcRows - 1) / kTcRows, 128, kTcSmem, m->s>>>(m->b_x, n, m->d_w, m->d_p, m->b_y,
+                                                                           m->d_err);
+        CKM(cudaGetLastError());
+        int herr = 0;
+        CKM(cudaMemcpyAsync(&herr, m->d_err, sizeof(int), cudaMemcpyDeviceToHost, m->s));
+        CKM(cudaMemcpyAsync(y_host, m->b_y, sizeof(float) * (size_t)n * kMlpOut, cudaMemcpyDeviceToHost, m->s));
+        CKM(cudaStreamSynchronize(m->s));
+        if (herr) {
+            set_error("tcgen05 inference: a wait on the MMA barrier expired");
+            return TSR_ERR_TIMEOUT;
+        }
+        return TSR_OK;
+    }
     if (fused) {
         k_mlp_infer<<<warps_grid(n), 128, 0, m->s>>>(m->b_x, n, m->d_w, m->d_p, m->b_y);
         CKM(cudaGetLastError());
