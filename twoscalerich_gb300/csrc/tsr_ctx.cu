@@ -46,6 +46,7 @@ struct ScenState {
     double dt = 0.0, beta = 0.0, nu = 0.0, eps = 0.0, errK = 0.0, vnw = 0.0, err = 0.0;
     bool last = false, happy = false, iterating = false;
     int m = 0, maxk = 0;
+    int m_prev = 0;              // Krylov dimension of the last accepted step
     std::vector<double> Hm, phi, cv, z;
 };
 
@@ -735,7 +736,8 @@ int alloc_work(tsr_ctx* c, int max_krylov)
         if ((rc = dev_alloc(c, sizeof(double) * (size_t)N * (size_t)(maxk + 1), &p))) return rc;
         c->d_V = (double*)p;
     }
-    c->HS = (long long)c->ldH * mk1 + S_COUNT;
+    // H block, the fixed slots, then the weighted norm of v_{j+1} for every j
+    c->HS = (long long)c->ldH * mk1 + S_COUNT + mk1;
     const size_t nscal = (size_t)c->HS * (size_t)S;
     if ((rc = dev_alloc(c, sizeof(double) * nscal, &p))) return rc;
     c->d_scal = (double*)p;
@@ -765,7 +767,7 @@ int alloc_work(tsr_ctx* c, int max_krylov)
     CK(cudaMallocHost(&c->h_eps, sizeof(double) * 3 * (size_t)S));
     CK(cudaMallocHost(&c->h_active, sizeof(int) * (size_t)S));
     CK(cudaMallocHost(&c->h_mint, sizeof(int) * 2 * (size_t)S));
-    CK(cudaMallocHost(&c->h_stage, sizeof(double) * (size_t)(c->ldH + 2) * S));
+    CK(cudaMallocHost(&c->h_stage, sizeof(double) * ((size_t)c->ldH * mk1 + mk1 + 4) * S));
     std::memset(c->h_eps, 0, sizeof(double) * 3 * (size_t)S);
     std::memset(c->h_coef, 0, sizeof(double) * (size_t)c->CS * S);
     std::memset(c->h_mint, 0, sizeof(int) * 2 * (size_t)S);
@@ -1159,7 +1161,7 @@ void arnoldi_kernels(tsr_ctx* c, int j, cudaEvent_t* ev, double frac)
         launch_mgs(c->d_w, V + (size_t)i * N, Hc + i, HS, vnext, g, res, HS, part, s);
     }
     launch_scale_wsq(c->d_w, scal_slot(c, S_HSQ), Hc + j + 1, scal_slot(c, S_IH), HS,
-                     V + (size_t)(j + 1) * N, c->d_winv, g, scal_slot(c, S_SV), part, s);
+                     V + (size_t)(j + 1) * N, c->d_winv, g, scal_slot(c, S_COUNT + j), part, s);
     if (ev) cudaEventRecordWithFlags(ev[3], s, cudaEventRecordExternal);
     else prof_end(c, pe);
 }
@@ -1287,86 +1289,101 @@ int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
         if ((rc = upload_eps(c))) return rc;
         if ((rc = set_active(c, arn))) return rc;
         launch_seg_scale(c->d_g0, scal_slot(c, S_IB), HS, V, c->seg, s);
-        for (int j = 0; j < c->maxk && narn > 0; ++j) {
+        // The first batch of Arnoldi steps is launched back to back up to the
+        // smallest Krylov dimension the iterating scenarios took last time;
+        // their columns are then checked in order exactly as if each had been
+        // read back alone (steps past a scenario's stopping point only write
+        // columns it never uses).  Further steps go one at a time.
+        int pred = c->maxk;
+        for (int q = 0; q < S; ++q)
+            if (arn[q]) pred = std::min(pred, std::max(1, c->sc[q].m_prev));
+        int j = 0;
+        while (j < c->maxk && narn > 0) {
+            const int nb = (j == 0) ? std::max(1, std::min(pred, c->maxk)) : 1;
             if ((rc = set_active(c, arn))) return rc;
             const double frac = (double)narn / S;
-            if (c->use_graphs) {
-                cudaGraphExec_t& ge = c->graphs[(size_t)j];
-                std::array<cudaEvent_t, 4>& ev = c->graph_ev[(size_t)j];
-                if (!ge) {
-                    for (auto& e : ev)
-                        if (!e) CK(cudaEventCreate(&e));
-                    set_counting(false);
-                    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-                    arnoldi_kernels(c, j, ev.data(), frac);
-                    cudaGraph_t g = nullptr;
-                    cudaError_t ce = cudaStreamEndCapture(s, &g);
-                    set_counting(true);
-                    CK(ce);
-                    CK(cudaGraphInstantiate(&ge, g, 0));
-                    CK(cudaGraphDestroy(g));
+            for (int jj = j; jj < j + nb; ++jj) {
+                if (c->use_graphs) {
+                    cudaGraphExec_t& ge = c->graphs[(size_t)jj];
+                    std::array<cudaEvent_t, 4>& ev = c->graph_ev[(size_t)jj];
+                    if (!ge) {
+                        for (auto& e : ev)
+                            if (!e) CK(cudaEventCreate(&e));
+                        set_counting(false);
+                        CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+                        arnoldi_kernels(c, jj, ev.data(), frac);
+                        cudaGraph_t g = nullptr;
+                        cudaError_t ce = cudaStreamEndCapture(s, &g);
+                        set_counting(true);
+                        CK(ce);
+                        CK(cudaGraphInstantiate(&ge, g, 0));
+                        CK(cudaGraphDestroy(g));
+                    }
+                    CK(cudaGraphLaunch(ge, s));
+                    add_launches(jj + 6);
+                } else {
+                    arnoldi_kernels(c, jj, nullptr, frac);
                 }
-                CK(cudaGraphLaunch(ge, s));
-                add_launches(j + 6);
-            } else {
-                arnoldi_kernels(c, j, nullptr, frac);
             }
-            for (int q = 0; q < S; ++q)
-                if (arn[q]) io.st[q].FuncEvals++;
             CK(cudaGetLastError());
-            // column j of every H and the weighted norms of v_{j+1}
-            const size_t row = (size_t)ldH + 1;
+            // columns j..j+nb-1 of every H and the weighted norms of v_{j+1..j+nb}
+            const size_t row = (size_t)nb * ldH + (size_t)nb;
             CK(cudaMemcpy2DAsync(c->h_stage, sizeof(double) * row, c->d_scal + (size_t)j * ldH,
-                                 sizeof(double) * HS, sizeof(double) * (size_t)(j + 2), (size_t)S,
+                                 sizeof(double) * HS, sizeof(double) * (size_t)nb * ldH, (size_t)S,
                                  cudaMemcpyDeviceToHost, s));
-            CK(cudaMemcpy2DAsync(c->h_stage + ldH, sizeof(double) * row, scal_slot(c, S_SV),
-                                 sizeof(double) * HS, sizeof(double), (size_t)S, cudaMemcpyDeviceToHost, s));
+            CK(cudaMemcpy2DAsync(c->h_stage + (size_t)nb * ldH, sizeof(double) * row, scal_slot(c, S_COUNT + j),
+                                 sizeof(double) * HS, sizeof(double) * (size_t)nb, (size_t)S,
+                                 cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
-            if (c->use_graphs && c->prof) {
-                std::array<cudaEvent_t, 4>& ev = c->graph_ev[(size_t)j];
-                float ta = 0.f, tb = 0.f;
-                CK(cudaEventElapsedTime(&ta, ev[0], ev[1]));
-                CK(cudaEventElapsedTime(&tb, ev[2], ev[3]));
-                c->prof_acc_ms[0] += ta;
-                c->prof_acc_bytes[0] += frac * g_bytes(c, true);
-                c->prof_acc_n[0] += 1;
-                c->prof_acc_ms[1] += tb;
-                c->prof_acc_bytes[1] += frac * 8.0 * (double)N * (double)(j + 3);
-                c->prof_acc_n[1] += 1;
-            }
-            for (int q = 0; q < S; ++q) {
-                if (!arn[q]) continue;
-                ScenState& z = c->sc[q];
-                const double* col = c->h_stage + (size_t)q * row;
-                double hs = 0.0;
-                for (int i = 0; i <= j; ++i) {
-                    z.Hm[(size_t)j * ldH + i] = col[i];
-                    hs = std::fma(col[i], col[i], hs);
+            for (int jj = j; jj < j + nb && narn > 0; ++jj) {
+                if (c->use_graphs && c->prof) {
+                    std::array<cudaEvent_t, 4>& ev = c->graph_ev[(size_t)jj];
+                    float ta = 0.f, tb = 0.f;
+                    CK(cudaEventElapsedTime(&ta, ev[0], ev[1]));
+                    CK(cudaEventElapsedTime(&tb, ev[2], ev[3]));
+                    c->prof_acc_ms[0] += ta;
+                    c->prof_acc_bytes[0] += frac * g_bytes(c, true);
+                    c->prof_acc_n[0] += 1;
+                    c->prof_acc_ms[1] += tb;
+                    c->prof_acc_bytes[1] += frac * 8.0 * (double)N * (double)(jj + 3);
+                    c->prof_acc_n[1] += 1;
                 }
-                const double hn = col[j + 1];
-                z.Hm[(size_t)j * ldH + j + 1] = hn;
-                const double Sv = col[ldH];
-                z.m = j + 1;
-                bool stop = false;
-                if (!(hn > 1e-12 * std::sqrt(std::fma(hn, hn, hs)))) {
-                    z.happy = true;
-                    stop = true;
-                } else if (!(z.m < opt->MinKrylov && z.m < z.maxk)) {
-                    z.vnw = std::sqrt(Sv / (double)Ns(q));
-                    if ((rc = phi_host(c, z, z.dt, z.m))) {
-                        fail(q, rc, "phipade: singular Pade denominator");
+                for (int q = 0; q < S; ++q) {
+                    if (!arn[q]) continue;
+                    ScenState& z = c->sc[q];
+                    io.st[q].FuncEvals++;
+                    const double* col = c->h_stage + (size_t)q * row + (size_t)(jj - j) * ldH;
+                    double hs = 0.0;
+                    for (int i = 0; i <= jj; ++i) {
+                        z.Hm[(size_t)jj * ldH + i] = col[i];
+                        hs = std::fma(col[i], col[i], hs);
+                    }
+                    const double hn = col[jj + 1];
+                    z.Hm[(size_t)jj * ldH + jj + 1] = hn;
+                    const double Sv = c->h_stage[(size_t)q * row + (size_t)nb * ldH + (size_t)(jj - j)];
+                    z.m = jj + 1;
+                    bool stop = false;
+                    if (!(hn > 1e-12 * std::sqrt(std::fma(hn, hn, hs)))) {
+                        z.happy = true;
                         stop = true;
-                    } else {
-                        z.errK = std::fabs(((z.dt * z.beta) * hn) * z.phi[(size_t)z.m - 1]) * z.vnw;
-                        if (z.errK <= kKrylovTol) stop = true;
+                    } else if (!(z.m < opt->MinKrylov && z.m < z.maxk)) {
+                        z.vnw = std::sqrt(Sv / (double)Ns(q));
+                        if ((rc = phi_host(c, z, z.dt, z.m))) {
+                            fail(q, rc, "phipade: singular Pade denominator");
+                            stop = true;
+                        } else {
+                            z.errK = std::fabs(((z.dt * z.beta) * hn) * z.phi[(size_t)z.m - 1]) * z.vnw;
+                            if (z.errK <= kKrylovTol) stop = true;
+                        }
+                    }
+                    if (z.m >= z.maxk) stop = true;
+                    if (stop) {
+                        arn[q] = 0;
+                        --narn;
                     }
                 }
-                if (z.m >= z.maxk) stop = true;
-                if (stop) {
-                    arn[q] = 0;
-                    --narn;
-                }
             }
+            j += nb;
         }
     }
     // Krylov error too large at the largest dimension: shorten the step
@@ -1520,6 +1537,7 @@ int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
             st.CurrentKryDim = z.m;
             st.NumSteps++;
             z.g0_valid = true;
+            z.m_prev = z.m;
         }
         pend.swap(next);
     }
