@@ -224,8 +224,10 @@ def test_relayout_matches_oracle_summary():
 @pytest.mark.slow
 def test_closure_end_to_end_and_ablation():
     """Train on plain runs of the 21 x 21 / 11 x 11 configuration (training
-    initial states from seeds 1001-1003), evaluate on the evaluation
-    state, compare with the plain run and with the untrained network."""
+    initial states from seeds 1001-1003), then (ablation) the held-out
+    error of the closure coefficients with the trained network against the
+    same network untrained, and the closure run (indicator 1e-3, fallback
+    on) against the plain run."""
     X, Y = [], []
     for seed in (1001, 1002, 1003):
         q = P.config1()
@@ -235,14 +237,21 @@ def test_closure_end_to_end_and_ablation():
         X.append(x)
         Y.append(y)
     X, Y = np.concatenate(X), np.concatenate(Y)
+    rng = np.random.default_rng(9)
+    hold = rng.permutation(X.shape[0])[:20000]
     model, hist, err = closure.train_model(X, Y, epochs=6, batch=2048, lr=2e-3, seed=1001)
     assert hist[-1] < hist[0]
+    untrained = closure.Mlp(closure.init_params(1001))
+    e_untrained = closure.heldout_error(untrained, model, X[hold], Y[hold])
+    untrained.close()
+    trained = closure.Mlp(model.params)
+    e_trained = closure.heldout_error(trained, model, X[hold], Y[hold])
+    trained.close()
+    assert e_trained["kQ_p50"] < 0.5 * e_untrained["kQ_p50"], (e_trained, e_untrained)
+    assert e_trained["kT_p50"] < 0.5 * e_untrained["kT_p50"], (e_trained, e_untrained)
     times = [0.25, 0.5, 1.0]
-    plain, wp, sp, fp, = P.config1(), None, None, None
-    rec_p, wall_p, steps_p, evals_p = closure.run_plain(plain, times)
-    rec_c, wall_c, steps_c, evals_c, frac = closure.run_closure(P.config1(), model, times)
-    rec_u, *_ = closure.run_closure(P.config1(), model, times, params=closure.init_params(7))
+    rec_p, wall_p, steps_p, evals_p = closure.run_plain(P.config1(), times)
+    rec_c, wall_c, steps_c, evals_c, frac = closure.run_closure(P.config1(), model, times, qfloor_rel=1.0)
     ep = [abs(c[1] - r[1]) / r[1] for c, r in zip(rec_c, rec_p)]
-    eu = [abs(c[1] - r[1]) / r[1] for c, r in zip(rec_u, rec_p)]
     assert max(ep) < 1e-2, ep
-    assert max(ep) < max(eu), (ep, eu)
+    assert all(0.0 <= f <= 1.0 for f in frac)
