@@ -155,6 +155,15 @@ int tsr_exprem_advance(tsr_ctx* ctx, double tend, const double* tspan,
                        exprem_stats_struct* stats, double* t_out);
 int tsr_exprem_store(tsr_ctx* ctx, double* u_host);
 
+/* ---- checkpoint / resume (no counterpart in the reference) --------------
+ * Saves the loaded state of every scenario (t, next step size, statistics,
+ * status, u) to a file, and restores it into a context of the same problem;
+ * stepping on continues the same trajectory (G(u) is evaluated once more
+ * after the restore, so FuncEvals is one higher per scenario).  stats: one
+ * per scenario.  Learned-closure contexts are not supported. */
+int tsr_checkpoint_save(tsr_ctx* ctx, const char* path, const exprem_stats_struct* stats);
+int tsr_checkpoint_load(tsr_ctx* ctx, const char* path, exprem_stats_struct* stats);
+
 /* ---- ensembles (no counterpart in the reference) ------------------------
  * A context built with tsr_model_ext.scenarios = S > 1 holds S independent
  * problems whose unknowns are laid out scenario by scenario.  G, Jv and

@@ -130,6 +130,8 @@ _SIGNATURES = {
     "tsr_exprem_advance": (C.c_int, [C.c_void_p, C.c_double, dp, dp, C.POINTER(ExpremOptions),
                                      C.POINTER(ExpremStats), dp]),
     "tsr_exprem_store": (C.c_int, [C.c_void_p, dp]),
+    "tsr_checkpoint_save": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(ExpremStats)]),
+    "tsr_checkpoint_load": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(ExpremStats)]),
     "tsr_num_scenarios": (C.c_int, [C.c_void_p]),
     "tsr_scenario_range": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_longlong),
                                      C.POINTER(C.c_longlong)]),

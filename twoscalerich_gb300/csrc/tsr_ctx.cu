@@ -2042,3 +2042,105 @@ extern "C" int tsr_cell_summary(tsr_ctx* c, const double* u, double* out)
     CK(cudaStreamSynchronize(c->stream));
     return TSR_OK;
 }
+
+// ---- checkpoint / resume -------------------------------------------------------
+// File layout (native byte order): "TSRCKPT1", int32 S, int64 N, then per
+// scenario t, status, m_prev and the exprem_stats fields (CurrentStep,
+// CurrentTime, CurrentKryDim, NumSteps, FuncEvals), then u (N doubles).
+// G(u) is not stored: the first step after a resume evaluates it again.
+
+namespace {
+struct CkptScen {
+    double t;
+    int32_t status, m_prev;
+    double cur_step, cur_time;
+    int32_t kry_dim, num_steps, func_evals, pad;
+};
+const char kCkptMagic[8] = {'T', 'S', 'R', 'C', 'K', 'P', 'T', '1'};
+}  // namespace
+
+extern "C" int tsr_checkpoint_save(tsr_ctx* c, const char* path, const exprem_stats_struct* stats)
+{
+    if (!c || !path || !stats || !c->sc[0].loaded) return TSR_ERR_ARG;
+    if (c->closure) {
+        set_error("checkpoints of learned-closure contexts are not supported");
+        return TSR_ERR_ARG;
+    }
+    std::vector<double> u((size_t)c->N);
+    CK(cudaMemcpyAsync(u.data(), c->d_u, sizeof(double) * u.size(), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    FILE* f = std::fopen(path, "wb");
+    if (!f) {
+        set_error(std::string("cannot open ") + path);
+        return TSR_ERR_IO;
+    }
+    const int32_t S = c->S;
+    const int64_t N = c->N;
+    bool ok = std::fwrite(kCkptMagic, 1, 8, f) == 8 && std::fwrite(&S, sizeof S, 1, f) == 1 &&
+              std::fwrite(&N, sizeof N, 1, f) == 1;
+    for (int q = 0; q < c->S && ok; ++q) {
+        CkptScen r{};
+        r.t = c->sc[q].t;
+        r.status = c->sc[q].status;
+        r.m_prev = c->sc[q].m_prev;
+        r.cur_step = stats[q].CurrentStep;
+        r.cur_time = stats[q].CurrentTime;
+        r.kry_dim = stats[q].CurrentKryDim;
+        r.num_steps = stats[q].NumSteps;
+        r.func_evals = stats[q].FuncEvals;
+        ok = std::fwrite(&r, sizeof r, 1, f) == 1;
+    }
+    ok = ok && std::fwrite(u.data(), sizeof(double), u.size(), f) == u.size();
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) {
+        set_error(std::string("write failed: ") + path);
+        return TSR_ERR_IO;
+    }
+    return TSR_OK;
+}
+
+extern "C" int tsr_checkpoint_load(tsr_ctx* c, const char* path, exprem_stats_struct* stats)
+{
+    if (!c || !path || !stats) return TSR_ERR_ARG;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) {
+        set_error(std::string("cannot open ") + path);
+        return TSR_ERR_IO;
+    }
+    char magic[8];
+    int32_t S = 0;
+    int64_t N = 0;
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kCkptMagic, 8) == 0 &&
+              std::fread(&S, sizeof S, 1, f) == 1 && std::fread(&N, sizeof N, 1, f) == 1;
+    if (!ok || S != c->S || N != c->N) {
+        std::fclose(f);
+        set_error("checkpoint does not match this context (format, scenarios or unknowns)");
+        return TSR_ERR_ARG;
+    }
+    std::vector<CkptScen> rs((size_t)S);
+    std::vector<double> u((size_t)N);
+    ok = std::fread(rs.data(), sizeof(CkptScen), rs.size(), f) == rs.size() &&
+         std::fread(u.data(), sizeof(double), u.size(), f) == u.size();
+    std::fclose(f);
+    if (!ok) {
+        set_error(std::string("truncated checkpoint: ") + path);
+        return TSR_ERR_IO;
+    }
+    CK(cudaMemcpyAsync(c->d_u, u.data(), sizeof(double) * u.size(), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int q = 0; q < S; ++q) {
+        ScenState& z = c->sc[q];
+        z.loaded = true;
+        z.t = rs[q].t;
+        z.status = rs[q].status;
+        z.m_prev = rs[q].m_prev;
+        z.g0_valid = false;
+        stats[q].CurrentStep = rs[q].cur_step;
+        stats[q].CurrentTime = rs[q].cur_time;
+        stats[q].CurrentKryDim = rs[q].kry_dim;
+        stats[q].NumSteps = rs[q].num_steps;
+        stats[q].FuncEvals = rs[q].func_evals;
+    }
+    c->last_u0 = nullptr;
+    return TSR_OK;
+}
