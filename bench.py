@@ -197,18 +197,21 @@ def workload(args, N):
             "parallelism": "replicas" if WORLD > 1 else "1 GPU"}
 
 
-def cpu_oracle_rate(p, n_evals, threads):
-    """G evaluations per second of the oracle's OpenMP Gfunc_parallel form."""
+def cpu_oracle_rate(p, n_evals, threads, min_seconds=10.0):
+    """G evaluations per second of the oracle's OpenMP Gfunc_parallel form:
+    at least n_evals evaluations and at least min_seconds of work."""
     import oracle
     o = oracle.Oracle(p, nthreads=threads, libm=True)
     g = np.empty(p.N)
     o.lib.oracle_g(o.h, o._p(p.u0), o._p(g), threads)       # first-touch / warm-up
     t0 = time.perf_counter()
-    for _ in range(n_evals):
+    n = 0
+    while n < n_evals or time.perf_counter() - t0 < min_seconds:
         o.lib.oracle_g(o.h, o._p(p.u0), o._p(g), threads)
+        n += 1
     el = time.perf_counter() - t0
     o.close()
-    return n_evals / el, el
+    return n / el, el, n
 
 
 def run_reference(args):
@@ -348,11 +351,10 @@ def run_ours(args):
     cpu = None
     if RANK == 0 and WORLD == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        rate, el = cpu_oracle_rate(p, args.cpu_evals, threads)
+        rate, el, n = cpu_oracle_rate(p, args.cpu_evals, threads, args.cpu_seconds)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": "%d G evaluations of the full workload by the oracle's OpenMP "
-                         "Gfunc_parallel form with C-library log/exp (%.1f s)"
-                         % (args.cpu_evals, el)}
+                         "Gfunc_parallel form with C-library log/exp (%.1f s)" % (n, el)}
     traffic = G_TRAFFIC_PER_UNKNOWN.get(args.n_micro) if args.config == 2 else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": WORLD, "steps": args.steps,
@@ -681,7 +683,8 @@ def main():
     ap.add_argument("--epochs", type=int, default=8)
     ap.add_argument("--log-seconds", type=float, default=45.0)
     ap.add_argument("--scenarios", type=int, default=64)
-    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0,
+                    help="minimum seconds of CPU work in the CPU baseline sample")
     ap.add_argument("--to-end", action="store_true",
                     help="config 4: also run every scenario to t_end (p50/p95 wall time)")
     ap.add_argument("--to-end-seconds", type=float, default=600.0,
