@@ -282,6 +282,11 @@ int tsr_profile_read(tsr_ctx* ctx, int category, double* ms, long long* count, d
  * default) or launch its kernels one by one (0).  Same results either way. */
 int tsr_set_graphs(tsr_ctx* ctx, int enable);
 
+/* Gram-Schmidt block of an Arnoldi step as one cooperative launch (1, the
+ * default) or as the j + 4 separate reduction launches (0).  Same results
+ * either way. */
+int tsr_set_fused_gs(tsr_ctx* ctx, int enable);
+
 /* Number of kernels the library has launched since it was loaded. */
 unsigned long long tsr_kernel_launches(void);
 

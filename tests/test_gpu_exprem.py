@@ -112,3 +112,19 @@ def test_dropin_gfunc_signature_path():
     capi.check(lib.tsr_gfunc_gpu(capi.ptr(g), capi.ptr(u), C.byref(p.ud)), "gfunc")
     assert np.array_equal(g, oracle.Oracle(p).g(u))
     lib.tsr_release_all()
+
+
+def test_fused_gram_schmidt_matches_separate_kernels():
+    """the cooperative single-launch Gram-Schmidt block gives the same
+    trajectory, bit for bit, as the separate reduction launches"""
+    p = P.config1()
+    p.tend = 0.05
+    p.tspan = np.array([1.0, 0.05])
+    out = []
+    for fused in (1, 0):
+        ctx = P.Context(p)
+        capi.check(ctx.lib.tsr_set_fused_gs(ctx.h, fused), "tsr_set_fused_gs")
+        out.append(P.run_to_end(ctx.exprem_step, p))
+    (ua, sa, sta, la), (ub, sb, stb, lb) = out
+    assert la == lb and np.array_equal(ua, ub) and np.array_equal(sa, sb)
+    assert sta.FuncEvals == stb.FuncEvals

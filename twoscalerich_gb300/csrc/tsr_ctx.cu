@@ -109,6 +109,12 @@ struct tsr_ctx {
     // one captured graph per Arnoldi index j, with event nodes timing its
     // Jv and its Gram-Schmidt block
     bool use_graphs = true;
+    // the Gram-Schmidt block of an Arnoldi step as one cooperative launch
+    bool fused_gs = true;
+    int gs_grid = 0;
+    long long pstride = 0;
+    unsigned int* d_gsbar = nullptr;
+    int* d_gserr = nullptr;
     std::vector<cudaGraphExec_t> graphs;
     std::vector<std::array<cudaEvent_t, 4>> graph_ev;
     double prof_acc_ms[2] = {0.0, 0.0}, prof_acc_bytes[2] = {0.0, 0.0};
@@ -759,8 +765,20 @@ int alloc_work(tsr_ctx* c, int max_krylov)
     if ((rc = make_seg(c, tstart, &c->seg_terms))) return rc;
     const int nb = std::max(std::max(c->seg.nblocks, c->seg_terms.nblocks),
                             reduction_blocks(std::max(N, (long long)c->Mn + c->Ne)));
-    if ((rc = dev_alloc(c, sizeof(double) * (size_t)nb, &p))) return rc;
+    // two partial buffers: the fused Gram-Schmidt kernel alternates them
+    if ((rc = dev_alloc(c, sizeof(double) * 2 * (size_t)nb, &p))) return rc;
     c->rw.partials = (double*)p;
+    c->pstride = nb;
+    if ((rc = dev_alloc(c, sizeof(unsigned int) * 4, &p))) return rc;
+    c->d_gsbar = (unsigned int*)p;
+    CK(cudaMemset(c->d_gsbar, 0, sizeof(unsigned int) * 4));
+    if ((rc = dev_alloc(c, sizeof(int) * 2, &p))) return rc;
+    c->d_gserr = (int*)p;
+    CK(cudaMemset(c->d_gserr, 0, sizeof(int) * 2));
+    c->gs_grid = gs_fused_grid(c->nsm);
+    if (c->gs_grid < 1) c->fused_gs = false;
+    if (const char* e = std::getenv("TSR_FUSED_GS"))
+        if (e[0] == '0') c->fused_gs = false;
     CK(cudaMallocHost(&c->h_scal, sizeof(double) * (size_t)c->ldH * 2));
     CK(cudaMallocHost(&c->h_coef, sizeof(double) * (size_t)c->CS * S));
     CK(cudaMallocHost(&c->h_flag, sizeof(int) * (size_t)S));
@@ -1132,7 +1150,8 @@ int phi_host(tsr_ctx* c, ScenState& z, double alpha, int m)
 // (finite differences), modified Gram-Schmidt against v_0..v_j,
 // h_{j+1,j} = ||w||, v_{j+1} = w / h_{j+1,j} and the weighted norm of
 // v_{j+1}.  ev (4 events or null) brackets the Jv and the Gram-Schmidt
-// block; otherwise the profiling pool does.  j + 6 kernels.
+// block; otherwise the profiling pool does.  3 kernels (fused Gram-Schmidt)
+// or j + 6.
 void arnoldi_kernels(tsr_ctx* c, int j, cudaEvent_t* ev, double frac)
 {
     const long long N = c->N;
@@ -1154,14 +1173,34 @@ void arnoldi_kernels(tsr_ctx* c, int j, cudaEvent_t* ev, double frac)
         prof_end(c, pe);
         pe = prof_begin(c, 1, frac * 8.0 * (double)N * (double)(j + 3));   // algorithmic minimum
     }
-    launch_dot(c->d_w, V, g, Hc, HS, part, s);
-    for (int i = 0; i <= j; ++i) {
-        const double* vnext = (i < j) ? V + (size_t)(i + 1) * N : nullptr;
-        double* res = (i < j) ? Hc + i + 1 : scal_slot(c, S_HSQ);
-        launch_mgs(c->d_w, V + (size_t)i * N, Hc + i, HS, vnext, g, res, HS, part, s);
+    if (c->fused_gs) {
+        GsArgs A{};
+        A.w = c->d_w;
+        A.V = V;
+        A.ldV = N;
+        A.Hc = Hc;
+        A.hsq = scal_slot(c, S_HSQ);
+        A.ih = scal_slot(c, S_IH);
+        A.sv = scal_slot(c, S_COUNT + j);
+        A.stride = HS;
+        A.j = j;
+        A.winv = c->d_winv;
+        A.partials = part;
+        A.pstride = c->pstride;
+        A.bar = c->d_gsbar;
+        A.err = c->d_gserr;
+        cudaMemsetAsync(c->d_gsbar, 0, 2 * sizeof(unsigned int), s);
+        launch_gs_fused(g, A, c->gs_grid, s);
+    } else {
+        launch_dot(c->d_w, V, g, Hc, HS, part, s);
+        for (int i = 0; i <= j; ++i) {
+            const double* vnext = (i < j) ? V + (size_t)(i + 1) * N : nullptr;
+            double* res = (i < j) ? Hc + i + 1 : scal_slot(c, S_HSQ);
+            launch_mgs(c->d_w, V + (size_t)i * N, Hc + i, HS, vnext, g, res, HS, part, s);
+        }
+        launch_scale_wsq(c->d_w, scal_slot(c, S_HSQ), Hc + j + 1, scal_slot(c, S_IH), HS,
+                         V + (size_t)(j + 1) * N, c->d_winv, g, scal_slot(c, S_COUNT + j), part, s);
     }
-    launch_scale_wsq(c->d_w, scal_slot(c, S_HSQ), Hc + j + 1, scal_slot(c, S_IH), HS,
-                     V + (size_t)(j + 1) * N, c->d_winv, g, scal_slot(c, S_COUNT + j), part, s);
     if (ev) cudaEventRecordWithFlags(ev[3], s, cudaEventRecordExternal);
     else prof_end(c, pe);
 }
@@ -1309,18 +1348,32 @@ int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
                     if (!ge) {
                         for (auto& e : ev)
                             if (!e) CK(cudaEventCreate(&e));
-                        set_counting(false);
-                        CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-                        arnoldi_kernels(c, jj, ev.data(), frac);
-                        cudaGraph_t g = nullptr;
-                        cudaError_t ce = cudaStreamEndCapture(s, &g);
-                        set_counting(true);
-                        CK(ce);
-                        CK(cudaGraphInstantiate(&ge, g, 0));
-                        CK(cudaGraphDestroy(g));
+                        for (int attempt = 0; attempt < 2 && !ge; ++attempt) {
+                            set_counting(false);
+                            CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+                            arnoldi_kernels(c, jj, ev.data(), frac);
+                            cudaGraph_t g = nullptr;
+                            cudaError_t ce = cudaStreamEndCapture(s, &g);
+                            set_counting(true);
+                            if (ce == cudaSuccess) ce = cudaGraphInstantiate(&ge, g, 0);
+                            if (g) cudaGraphDestroy(g);
+                            if (ce != cudaSuccess) {
+                                // a cooperative launch that cannot be captured:
+                                // capture the separate Gram-Schmidt kernels
+                                ge = nullptr;
+                                cudaGetLastError();
+                                if (!c->fused_gs || attempt == 1) CK(ce);
+                                c->fused_gs = false;
+                                for (auto& x : c->graphs)
+                                    if (x) {
+                                        cudaGraphExecDestroy(x);
+                                        x = nullptr;
+                                    }
+                            }
+                        }
                     }
                     CK(cudaGraphLaunch(ge, s));
-                    add_launches(jj + 6);
+                    add_launches(c->fused_gs ? 3 : jj + 6);
                 } else {
                     arnoldi_kernels(c, jj, nullptr, frac);
                 }
@@ -1335,6 +1388,15 @@ int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
                                  sizeof(double) * HS, sizeof(double) * (size_t)nb, (size_t)S,
                                  cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
+            if (c->fused_gs) {
+                int e = 0;
+                CK(cudaMemcpy(&e, c->d_gserr, sizeof(int), cudaMemcpyDeviceToHost));
+                if (e) {
+                    set_error("Gram-Schmidt: a grid barrier wait expired");
+                    cudaMemset(c->d_gserr, 0, sizeof(int));
+                    return TSR_ERR_TIMEOUT;
+                }
+            }
             for (int jj = j; jj < j + nb && narn > 0; ++jj) {
                 if (c->use_graphs && c->prof) {
                     std::array<cudaEvent_t, 4>& ev = c->graph_ev[(size_t)jj];
@@ -1829,6 +1891,19 @@ extern "C" int tsr_set_graphs(tsr_ctx* c, int enable)
 {
     if (!c) return TSR_ERR_ARG;
     c->use_graphs = enable != 0;
+    return TSR_OK;
+}
+
+extern "C" int tsr_set_fused_gs(tsr_ctx* c, int enable)
+{
+    if (!c) return TSR_ERR_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    c->fused_gs = enable != 0 && c->gs_grid > 0;
+    for (auto& g : c->graphs)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
     return TSR_OK;
 }
 

@@ -181,6 +181,29 @@ void launch_mgs(double* w, const double* vi, const double* h, int hstride, const
 void launch_scale_wsq(const double* w, const double* hsq, double* hn, double* ih, int stride,
                       double* v, const double* winv, const SegInfo& g, double* res, double* partials,
                       cudaStream_t s);
+// The Gram-Schmidt block of Arnoldi step j in one cooperative launch
+// (results identical to launch_dot + j+1 launch_mgs + launch_scale_wsq):
+// column j of scenario s at Hc + s*stride, h_{j+1,j}^2 at hsq, 1/h at ih,
+// the weighted norm of v_{j+1} at sv (all strided by `stride`).
+struct GsArgs {
+    double* w;
+    double* V;
+    long long ldV;
+    double* Hc;
+    double* hsq;
+    double* ih;
+    double* sv;
+    int stride;
+    int j;
+    const double* winv;
+    double* partials;           // 2 x pstride
+    long long pstride;
+    unsigned int* bar;          // [2] barrier count and generation
+    int* err;                   // set if a barrier wait expired
+};
+int gs_fused_grid(int nsm);     // co-resident CTAs of the fused kernel
+cudaError_t launch_gs_fused(const SegInfo& g, const GsArgs& A, int max_grid, cudaStream_t s);
+
 // b = a and d = c on the active segments
 void launch_seg_copy2(const double* a, double* b, const double* c, double* d, const SegInfo& g,
                       cudaStream_t s);

@@ -21,6 +21,7 @@
 // explicit fma(), matching the host evaluation operation for operation.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <string>
 
 #include "tsr_device.h"
@@ -795,6 +796,247 @@ void launch_err(const double* g1, const double* g0, const double* V, long long l
                 const SegInfo& g, double* res, int rstride, double* partials, cudaStream_t s)
 {
     run_reduce(TermErr{g1, g0, V, ldV, z, zstride, mz, dt3, dstride, winv}, g, res, rstride, partials, s);
+}
+
+// ---- fused Gram-Schmidt block of one Arnoldi step -----------------------------
+// One cooperative launch does what the dot, the j+1 MGS passes, the square
+// root and the scaling do as separate launches: pass p over every chunk of
+// every active segment, a grid barrier, and so on.  Each chunk's partial sum
+// and each segment's total are formed exactly as in k_reduce (same thread
+// mapping, same trees), so the results are the same bits; every CTA forms
+// the totals it needs from the previous pass's partials itself (partials
+// alternate between two buffers, so no extra barrier is needed).
+static constexpr long long kGridSpinLimit = 1LL << 22;
+
+__device__ __forceinline__ SegBlock seg_block_at(const SegInfo& g, int b)
+{
+    SegBlock r;
+    if (g.start) {
+        r.s = g.blkseg[b];
+        r.lo = g.start[r.s];
+        r.hi = g.start[r.s + 1];
+        r.b0 = g.block0[r.s];
+        r.nb = g.block0[r.s + 1] - r.b0;
+        r.lb = b - r.b0;
+    } else {
+        r.s = 0;
+        r.lo = 0;
+        r.hi = g.n1;
+        r.b0 = 0;
+        r.nb = g.nblocks;
+        r.lb = b;
+    }
+    return r;
+}
+
+// grid-wide barrier with a bounded wait; false (and *err set) if it expired
+__device__ __forceinline__ bool grid_barrier(unsigned int* count, unsigned int* gen, unsigned int nblk, int* err)
+{
+    __shared__ int ok_s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok_s = 1;
+        volatile unsigned int* vg = gen;
+        const unsigned int g0 = *vg;
+        __threadfence();
+        if (atomicAdd(count, 1u) == nblk - 1) {
+            atomicExch(count, 0u);
+            __threadfence();
+            atomicAdd(gen, 1u);
+        } else {
+            long long it = 0;
+            while (*vg == g0) {
+                if (++it > kGridSpinLimit) {
+                    atomicOr(err, 1);
+                    ok_s = 0;
+                    break;
+                }
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok_s != 0;
+}
+
+template <class Term>
+__device__ __forceinline__ double chunk_partial(const Term& term, const SegBlock& B, double* ws)
+{
+    const long long base = B.lo + (long long)B.lb * kRedChunk + threadIdx.x;
+    double a = 0.0;
+#pragma unroll 4
+    for (int q = 0; q < kRedChunk / kRedThreads; ++q) {
+        const long long i = base + (long long)q * kRedThreads;
+        if (i < B.hi) a = term(B.s, i, a);
+    }
+    return block_sum_256(a, ws);
+}
+
+// the segment's total from its chunk partials (as the last block of
+// k_reduce forms it), broadcast to every thread
+__device__ __forceinline__ double segment_total(const SegBlock& B, const double* partials, double* ws, double* bc)
+{
+    double a = 0.0;
+    for (int i = threadIdx.x; i < B.nb; i += kRedThreads) a = a + __ldcg(partials + B.b0 + i);
+    const double t = block_sum_256(a, ws);
+    if (threadIdx.x == 0) *bc = t;
+    __syncthreads();
+    const double r = *bc;
+    __syncthreads();
+    return r;
+}
+
+// CLUSTER: the grid is one thread-block cluster (at most 16 CTAs) and the
+// passes are separated by the hardware cluster barrier; otherwise by the
+// bounded global-memory barrier of a cooperative launch.
+template <bool CLUSTER>
+__global__ void __launch_bounds__(kRedThreads) k_gs_fused(SegInfo g, GsArgs A)
+{
+    __shared__ double ws[8];
+    __shared__ double bc;
+    const int j = A.j;
+    for (int p = 0; p <= j + 2; ++p) {
+        double* part = A.partials + (size_t)(p & 1) * A.pstride;
+        const double* prev = A.partials + (size_t)((p + 1) & 1) * A.pstride;
+        int cs = -1;          // segment whose previous-pass total is cached
+        double ch = 0.0;
+        for (int b = blockIdx.x; b < g.nblocks; b += gridDim.x) {
+            const SegBlock B = seg_block_at(g, b);
+            if (g.active && !g.active[B.s]) continue;
+            const long long so = (long long)B.s * A.stride;
+            double r;
+            if (p == 0) {
+                r = chunk_partial(TermDot{A.w, A.V}, B, ws);
+            } else {
+                if (B.s != cs) {
+                    ch = segment_total(B, prev, ws, &bc);     // total of pass p-1
+                    cs = B.s;
+                }
+                const double h = ch;
+                const bool writer = (b == B.b0) && threadIdx.x == 0;
+                if (p <= j + 1) {
+                    // h = H(p-1, j); w -= h v_{p-1}; dot with v_p (or with w after the last)
+                    if (writer) A.Hc[so + p - 1] = h;
+                    double* hp = &bc;     // TermMgs reads h through a pointer
+                    (void)hp;
+                    const double* vi = A.V + (size_t)(p - 1) * A.ldV;
+                    const double* vn = (p <= j) ? A.V + (size_t)p * A.ldV : nullptr;
+                    struct {
+                        double* w;
+                        const double* vi;
+                        double h;
+                        const double* vn;
+                        __device__ double operator()(int, long long i, double a) const
+                        {
+                            double wn = fma(-h, vi[i], w[i]);
+                            w[i] = wn;
+                            return fma(wn, vn ? vn[i] : wn, a);
+                        }
+                    } t{A.w, vi, h, vn};
+                    r = chunk_partial(t, B, ws);
+                } else {
+                    // h = ||w||^2: H(j+1, j) = sqrt, v_{j+1} = w / H(j+1, j), weighted norm
+                    const double hn = sqrt(h);
+                    const double ih = 1.0 / hn;
+                    if (writer) {
+                        A.hsq[so] = h;
+                        A.Hc[so + j + 1] = hn;
+                        A.ih[so] = ih;
+                    }
+                    double* v = A.V + (size_t)(j + 1) * A.ldV;
+                    struct {
+                        const double* w;
+                        double ih;
+                        double* v;
+                        const double* winv;
+                        __device__ double operator()(int, long long i, double a) const
+                        {
+                            double vv = w[i] * ih;
+                            v[i] = vv;
+                            double rr = vv * winv[i];
+                            return fma(rr, rr, a);
+                        }
+                    } t{A.w, ih, v, A.winv};
+                    r = chunk_partial(t, B, ws);
+                }
+            }
+            if (threadIdx.x == 0) part[b] = r;
+        }
+        if (CLUSTER) {
+            __threadfence();
+            asm volatile("barrier.cluster.arrive.release.aligned;\n"
+                         "barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+        } else if (!grid_barrier(A.bar, A.bar + 1, gridDim.x, A.err)) {
+            return;
+        }
+    }
+    // the weighted norm of v_{j+1} (total of the last pass)
+    const double* last = A.partials + (size_t)((j + 2) & 1) * A.pstride;
+    for (int b = blockIdx.x; b < g.nblocks; b += gridDim.x) {
+        const SegBlock B = seg_block_at(g, b);
+        if (g.active && !g.active[B.s]) continue;
+        if (b != B.b0) continue;
+        const double sv = segment_total(B, last, ws, &bc);
+        if (threadIdx.x == 0) A.sv[(long long)B.s * A.stride] = sv;
+    }
+}
+
+static constexpr int kGsMaxCluster = 16;
+static int g_gs_cluster_max = 0;    // largest cluster the device schedules for the fused kernel
+
+int gs_fused_grid(int nsm)
+{
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_gs_fused<false>, kRedThreads, 0) != cudaSuccess)
+        return 0;
+    // clusters of more than 8 CTAs are a non-portable size: use them only if
+    // the device can schedule one
+    g_gs_cluster_max = 0;
+    if (cudaFuncSetAttribute(k_gs_fused<true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+        cudaGetLastError();
+    for (int cs : {kGsMaxCluster, 8}) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)cs);
+        cfg.blockDim = dim3(kRedThreads);
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)cs;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int nc = 0;
+        if (cudaOccupancyMaxActiveClusters(&nc, k_gs_fused<true>, &cfg) == cudaSuccess && nc > 0) {
+            g_gs_cluster_max = cs;
+            break;
+        }
+        cudaGetLastError();
+    }
+    return occ * nsm;
+}
+
+cudaError_t launch_gs_fused(const SegInfo& g, const GsArgs& A, int max_grid, cudaStream_t s)
+{
+    count();
+    cudaLaunchConfig_t cfg = {};
+    const int grid = std::min(g.nblocks, max_grid);
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kRedThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (grid <= g_gs_cluster_max) {
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)grid;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        return cudaLaunchKernelEx(&cfg, k_gs_fused<true>, g, A);
+    }
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    return cudaLaunchKernelEx(&cfg, k_gs_fused<false>, g, A);
 }
 
 // ---- elementwise, over segments (same block mapping as the reductions) -------
