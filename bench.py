@@ -613,7 +613,8 @@ def run_closure_bench(args):
 
     def attempt(**kw):
         try:
-            return closure.run_closure(mk(), model, times, thr=args.indicator, qfloor_rel=1.0, **kw), None
+            return closure.run_closure(mk(), model, times, thr=args.indicator, qfloor_rel=1.0,
+                                       t_switch=args.closure_start, **kw), None
         except TsrError as e:
             return None, str(e)
     res, fail_c = attempt()
@@ -639,7 +640,7 @@ def run_closure_bench(args):
                    "|dkQ| |H_c - h| <= thr * max|Q(t=0)| per step", "macro_nodes":
                    "%dx%d" % (args.n_macro, args.n_macro), "micro_nodes_per_cell":
                    "%dx%d" % (args.n_micro, args.n_micro), "cells": 2 * (args.n_macro - 1) ** 2,
-                   "output_times_d": times, "indicator": args.indicator,
+                   "output_times_d": times, "indicator": args.indicator, "closure_start_d": args.closure_start,
                    "network": "6 -> 4 x 64 SiLU -> 2, bf16 mma.sync, fp32 accumulation"},
         "plain": {"wall_s": wp, "steps": sp, "g_evals": fp, "water": [r[1] for r in rp]},
         "closure": {"wall_s": wc, "steps": sc, "g_evals": fc, "fallback_fraction": frac,
@@ -680,6 +681,8 @@ def main():
                          "4: 64-scenario ensemble of 51x51 x 15x15; 5: learned closure, 301x301")
     ap.add_argument("--times", default="1e-4,2.5e-4,5e-4", help="config 5 output times [d]")
     ap.add_argument("--indicator", type=float, default=1e-3)
+    ap.add_argument("--closure-start", type=float, default=0.0,
+                    help="config 5: plain method up to this time [d], then the closure")
     ap.add_argument("--epochs", type=int, default=8)
     ap.add_argument("--log-seconds", type=float, default=45.0)
     ap.add_argument("--scenarios", type=int, default=64)

@@ -308,15 +308,27 @@ def run_plain(p, times, max_steps=1000000):
 
 
 def run_closure(p, model, times, thr=1e-3, qfloor_rel=1e-3, auto_fallback=True, max_steps=1000000,
-                params=None):
-    """The same run with the learned closure: every cell starts learned;
-    flagged cells fall back to their micro meshes.  Returns (records, wall
-    seconds, steps, G evaluations, fallback fraction per record time)."""
+                params=None, t_switch=0.0):
+    """The same run with the learned closure: the plain method up to
+    t_switch (0: none), then every cell learned; flagged cells fall back to
+    their micro meshes.  Returns (records, wall seconds, steps, G
+    evaluations, fallback fraction per record time); the wall time includes
+    the plain start."""
     p.set_learned(np.zeros(p.Ne, dtype=np.int32))      # full layout, closure enabled
     ctx = P.Context(p)
     lib = ctx.lib
     net = Mlp(model.params if params is None else params)
     check(lib.tsr_exprem_load(ctx.h, ptr(p.u0), 0.0), "load")
+    st = capi.ExpremStats()
+    t = C.c_double(0.0)
+    tspan = np.array([0.0])
+    check(lib.tsr_sync(ctx.h), "sync")
+    w_start = time.perf_counter()
+    while t.value < t_switch and st.NumSteps < max_steps:
+        check(lib.tsr_exprem_advance(ctx.h, t_switch, ptr(tspan), None, C.byref(p.options), C.byref(st),
+                                     C.byref(t)), "advance")
+    check(lib.tsr_sync(ctx.h), "sync")
+    wall0 = time.perf_counter() - w_start
     # flux floor: a fraction of the largest plain exchange inflow at t = 0
     summ = np.empty(5 * p.Ne)
     check(lib.tsr_cell_summary(ctx.h, None, ptr(summ)), "summary")
@@ -331,15 +343,12 @@ def run_closure(p, model, times, thr=1e-3, qfloor_rel=1e-3, auto_fallback=True, 
     f0 = features(S0[:, 0], np.full((p.Ne, 3), np.nan), [0.0, -1e30, -1e30, -1e30], S0[:, 1], S0[:, 4])
     z0 = (f0 - model.fmu) / model.fsd
     ood0 = [float(np.mean((z0[:, i] < model.zlo[i]) | (z0[:, i] > model.zhi[i]))) for i in range(N_FEAT)]
-    st = capi.ExpremStats()
-    t = C.c_double(0.0)
     nf = C.c_int()
-    tspan = np.array([0.0])
     rec, frac = [], []
     learned = np.empty(p.Ne, dtype=np.int32)
     check(lib.tsr_sync(ctx.h), "sync")
     w0 = time.perf_counter()
-    wall = 0.0
+    wall = wall0
     nfl = []
     for tk in times:
         while t.value < tk and st.NumSteps < max_steps:
