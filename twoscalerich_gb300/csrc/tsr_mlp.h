@@ -23,31 +23,6 @@ constexpr int kMlpInPad = 16;
 constexpr int kMlpHidden = 64;
 constexpr int kMlpOut = 2;
 constexpr int kMlpOutPad = 8;
-constexpr int kMlpLayers = 5;
-
-struct MlpLayout {
-    int nin[kMlpLayers], nout[kMlpLayers];
-    int w[kMlpLayers], b[kMlpLayers];   // offsets into the parameter block
-    int total;
-};
-
-__host__ __device__ inline MlpLayout mlp_layout()
-{
-    MlpLayout L{};
-    const int nin[kMlpLayers] = {kMlpInPad, kMlpHidden, kMlpHidden, kMlpHidden, kMlpHidden};
-    const int nout[kMlpLayers] = {kMlpHidden, kMlpHidden, kMlpHidden, kMlpHidden, kMlpOutPad};
-    int off = 0;
-    for (int l = 0; l < kMlpLayers; ++l) {
-        L.nin[l] = nin[l];
-        L.nout[l] = nout[l];
-        L.w[l] = off;
-        off += nin[l] * nout[l];
-        L.b[l] = off;
-        off += nout[l];
-    }
-    L.total = off;
-    return L;
-}
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
 {
