@@ -287,6 +287,13 @@ int tsr_set_graphs(tsr_ctx* ctx, int enable);
  * either way. */
 int tsr_set_fused_gs(tsr_ctx* ctx, int enable);
 
+/* Failure paths of the bounded device waits, run on purpose (tests):
+ * which = 0, the grid barrier of the fused Gram-Schmidt kernel with a CTA
+ * that never arrives; 1, the tensor-core MMA barrier with nothing arriving.
+ * Returns TSR_ERR_TIMEOUT (the wait ran out and raised its error flag; no
+ * fault, the device stays usable). */
+int tsr_wait_probe(int which);
+
 /* Number of kernels the library has launched since it was loaded. */
 unsigned long long tsr_kernel_launches(void);
 

@@ -71,3 +71,16 @@ def test_gpu_status_codes():
     with pytest.raises(capi.TsrError) as e:
         P.run_to_end(ctx3.exprem_step, p)
     assert e.value.code == 9
+
+
+@pytest.mark.gpu
+def test_bounded_waits_expire_without_fault():
+    """a wait that can never complete (a CTA that never reaches the grid
+    barrier; an MMA barrier nothing arrives on) runs out, raises its flag
+    and returns TSR_ERR_TIMEOUT; the device and a context stay usable"""
+    lib = capi.load()
+    assert lib.tsr_wait_probe(0) == 4                       # TSR_ERR_TIMEOUT
+    assert lib.tsr_wait_probe(1) == 4
+    p = _problem()
+    ctx = P.Context(p)
+    assert np.array_equal(ctx.g(p.u0), oracle.Oracle(p).g(p.u0))

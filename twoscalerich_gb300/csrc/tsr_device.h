@@ -202,6 +202,9 @@ struct GsArgs {
     int* err;                   // set if a barrier wait expired
 };
 int gs_fused_grid(int nsm);     // co-resident CTAs of the fused kernel
+// the grid barrier's bounded wait run out on purpose (a CTA that never
+// arrives); *timed_out = 1 if the wait expired and raised its flag
+int barrier_probe(int* timed_out);
 cudaError_t launch_gs_fused(const SegInfo& g, const GsArgs& A, int max_grid, cudaStream_t s);
 
 // b = a and d = c on the active segments

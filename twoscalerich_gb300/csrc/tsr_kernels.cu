@@ -981,6 +981,36 @@ __global__ void __launch_bounds__(kRedThreads) k_gs_fused(SegInfo g, GsArgs A)
     }
 }
 
+// Failure-path probe of the bounded grid barrier: CTA 1 leaves without
+// arriving, so CTA 0's wait must run out and raise *err.
+__global__ void k_barrier_probe(unsigned int* bar, int* err)
+{
+    if (blockIdx.x == 1) return;
+    grid_barrier(bar, bar + 1, 2u, err);
+}
+
+int barrier_probe(int* timed_out)
+{
+    unsigned int* bar = nullptr;
+    int* err = nullptr;
+    if (cudaMalloc(&bar, 2 * sizeof(unsigned int)) != cudaSuccess) return 1;
+    if (cudaMalloc(&err, sizeof(int)) != cudaSuccess) {
+        cudaFree(bar);
+        return 1;
+    }
+    cudaMemset(bar, 0, 2 * sizeof(unsigned int));
+    cudaMemset(err, 0, sizeof(int));
+    k_barrier_probe<<<2, 32>>>(bar, err);
+    cudaError_t e = cudaDeviceSynchronize();
+    int h = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&h, err, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(bar);
+    cudaFree(err);
+    if (e != cudaSuccess) return 1;
+    *timed_out = h;
+    return 0;
+}
+
 static constexpr int kGsMaxCluster = 16;
 static int g_gs_cluster_max = 0;    // largest cluster the device schedules for the fused kernel
 

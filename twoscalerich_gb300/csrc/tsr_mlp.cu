@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "../../include/tsr_capi.h"
+#include "tsr_device.h"
 #include "tsr_internal.h"
 #include "tsr_mlp.h"
 #include "tsr_mlp_tc.cuh"
@@ -346,6 +347,23 @@ __global__ void __launch_bounds__(128) k_mlp_infer_tc(const float* __restrict__ 
     tc_free(tmem);
 }
 
+// Failure-path probe of the MMA barrier wait: an mbarrier nothing arrives
+// on, polled `limit` times like the network's waits; *err = 1 on expiry.
+__global__ void k_mbar_probe(long long limit, int* err)
+{
+    __shared__ __align__(8) unsigned long long bar;
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(&bar)), "r"(1u) : "memory");
+        long long spins = 0;
+        while (!bar_try_wait(smem_u32(&bar), 0u)) {
+            if (++spins > limit) {
+                *err = 1;
+                break;
+            }
+        }
+    }
+}
+
 }  // namespace
 
 struct tsr_mlp {
@@ -662,5 +680,34 @@ extern "C" int tsr_mlp_train(tsr_mlp* m, int epochs, int batch, float lr, float 
         if (loss_hist) loss_hist[e] = (float)(s / (double)nb);
     }
     cudaFreeHost(h_loss);
+    return TSR_OK;
+}
+
+// Bounded-wait failure paths, run on purpose: which = 0 the grid barrier of
+// the fused Gram-Schmidt kernel (a CTA that never arrives), 1 the tensor-core
+// MMA barrier (nothing arrives).  Returns TSR_ERR_TIMEOUT when the wait ran
+// out and raised its flag, as it must; the context stays usable.
+extern "C" int tsr_wait_probe(int which)
+{
+    int timed_out = 0;
+    if (which == 0) {
+        if (tsr::barrier_probe(&timed_out)) {
+            set_error("wait probe: CUDA error");
+            return TSR_ERR_CUDA;
+        }
+    } else {
+        int* err = nullptr;
+        CKM(cudaMalloc(&err, sizeof(int)));
+        CKM(cudaMemset(err, 0, sizeof(int)));
+        k_mbar_probe<<<1, 32>>>(1LL << 14, err);
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e == cudaSuccess) e = cudaMemcpy(&timed_out, err, sizeof(int), cudaMemcpyDeviceToHost);
+        cudaFree(err);
+        CKM(e);
+    }
+    if (timed_out) {
+        set_error("wait probe: the bounded wait expired");
+        return TSR_ERR_TIMEOUT;
+    }
     return TSR_OK;
 }

@@ -32,7 +32,7 @@ namespace tsr {
 constexpr int kTcRows = 128;            // rows per CTA (the MMA's M)
 constexpr int kTcCols = 64;             // tensor-memory columns allocated
 constexpr int kTcOutN = 16;             // last layer's N (2 outputs, zero padded)
-constexpr long long kTcSpinLimit = 1LL << 26;
+constexpr long long kTcSpinLimit = 1LL << 20;   // polls of the MMA barrier (each may suspend briefly)
 
 // shared-memory plan (bytes): weight tiles of the 5 layers, the activation
 // tile, the mbarrier and the tensor-memory address
