@@ -506,11 +506,14 @@ static double micro_cell(const oracle_problem* P, const double* x, int k, double
     interp_coeffs(P, x, k, al);
     const double cx = M->centroid_elements[k], cy = M->centroid_elements[Ne + k];
     if (P->learned && P->learned[k]) {
-        /* learned closure: one unknown, the interior mean water content */
+        /* learned closure: one unknown, the interior mean water content th,
+         * relaxing towards the water content theta_B(H_c) of the macro head
+         * at the cell centre */
         const double th = x[off];
-        const double hb = vg_head(th, pB);
         const double Hc = interp_at(P->nv, al, cx, cy);
-        const double d = Hc - hb;
+        double K, Cn, Cd, Se;
+        vg_eval(Hc, pB, &K, &Cn, &Cd, &Se);
+        const double d = fma(pB->dth, Se, pB->thr) - th;
         const double kQ = P->kappa ? P->kappa[2 * k] : 0.0;
         const double kT = P->kappa ? P->kappa[2 * k + 1] : 0.0;
         g[off] = kT * d;

@@ -72,8 +72,16 @@ def test_learned_cells_in_oracle_g_and_water():
     Hc, th, rate, Q, hb = S[k].T
     assert np.array_equal(th, u[p.cell_off[k]])
     assert np.array_equal(rate, g[p.cell_off[k]])
-    assert np.array_equal(rate, kappa[2 * k + 1] * (Hc - hb))
-    assert np.array_equal(Q, kappa[2 * k] * (Hc - hb))
+    # relaxation towards theta_B(H_c): the oracle's own water content at H_c
+    lib = oracle.load()
+    soil = P.make_soil(**P.SOIL_B)
+    out = np.empty(3)
+    thH = np.empty(k.size)
+    for i, h in enumerate(Hc):
+        lib.oracle_vg(C.byref(soil), 0.0, h, out.ctypes.data_as(capi.dp))
+        thH[i] = out[2]
+    assert np.array_equal(rate, kappa[2 * k + 1] * (thH - th))
+    assert np.array_equal(Q, kappa[2 * k] * (thH - th))
     w = orc.water(u)
     assert np.isfinite(w) and w > 0
 
@@ -130,16 +138,17 @@ def test_samples_features_and_targets():
     rng = np.random.default_rng(2)
     logs = []
     for n in range(5):
-        S = np.zeros((p.Ne, 5), dtype=np.float32)
+        S = np.zeros((p.Ne, 5), dtype=np.float64)
         S[:, 0] = -1.0 - 0.1 * n                     # H_c falling 0.1 per step
         S[:, 4] = -2.0                               # h(theta)
         S[:, 1] = 0.2
-        S[:, 3] = 0.05 * (S[:, 0] - S[:, 4])         # Q = 0.05 (H_c - h)
-        S[:, 2] = 0.5 * (S[:, 0] - S[:, 4])
-        logs.append((0.1 * n, S))
+        d = closure.theta_of(S[:, 0], P.SOIL_B) - S[:, 1]
+        S[:, 3] = 0.05 * d                           # Q = 0.05 (theta_B(H_c) - theta)
+        S[:, 2] = 0.5 * d
+        logs.append((0.1 * n, S.astype(np.float32)))
     X, Y = closure.samples(p, logs)
     assert X.shape[1] == 8 and Y.shape[1] == 2
-    assert np.allclose(Y[:, 0], np.log(0.05), atol=1e-6)
+    assert np.allclose(Y[:, 0], np.log(0.05), atol=1e-5)
     # rate features: asinh(-0.1 / 0.1) = asinh(-1) once the history exists
     last = X[-p.Ne:]
     assert np.allclose(last[:, 1:4], np.arcsinh(-1.0), atol=1e-5)

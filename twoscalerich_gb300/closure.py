@@ -2,10 +2,13 @@
 
 A learned cell carries one unknown, the mean water content theta of its
 inclusion's interior nodes.  With H_c the macro head at the cell centre and
-h(theta) the head of material B at that water content, the closure gives
+theta_B(H_c) the water content of material B at that head, the closure is a
+relaxation in water content,
 
-    exchange inflow      Q           = kQ (H_c - h(theta))
-    interior water rate  d theta/dt  = kT (H_c - h(theta)),
+    exchange inflow      Q           = kQ (theta_B(H_c) - theta)
+    interior water rate  d theta/dt  = kT (theta_B(H_c) - theta),
+
+smooth in every input and linear in theta.
 
 and the network predicts the coefficients from six inputs -- the macro
 head, its rates over the last three accepted steps, theta and h(theta):
@@ -20,16 +23,16 @@ Jacobian of EXPREM sees the exact linearisation of the closure.
 
 After every step an a-posteriori indicator compares the inflow the held
 coefficients gave with the one the network gives at the new state,
-|kQ' - kQ| |H_c - h| / max(kQ' |H_c - h|, q_floor) (from a cell's second
-learned step on), and flags inputs outside
+|kQ' - kQ| |d| / max(kQ' |d|, q_floor), d = theta_B(H_c) - theta (from a
+cell's second learned step on), and flags inputs outside
 the training range; flagged cells fall back to their micro meshes and the
 plain FP64 cell kernel for the rest of the run.
 
 Training data are logged from plain-method runs: after every accepted step
 the per-cell summary (tsr_cell_summary) gives H_c, theta, d theta/dt and Q
 of every cell, from which the inputs and the targets
-y1 = log(Q / (H_c - h)), y2 = log(s^2 A_int (d theta/dt) / (H_c - h)) are
-formed where both ratios are positive.
+y1 = log(Q / d), y2 = log(s^2 A_int (d theta/dt) / d) are formed where both
+ratios are positive.
 """
 import ctypes as C
 import time
@@ -53,6 +56,14 @@ def interior_area(p):
     a = float(cv[bnd != 1].sum())
     s = p._scale if p._scale is not None else np.ones(p.Ne)
     return (s * s) * a
+
+
+def theta_of(h, soil):
+    """water content of a van Genuchten material (dict) at head h"""
+    h = np.asarray(h, dtype=np.float64)
+    m = 1.0 - 1.0 / soil["n"]
+    Se = np.where(h < 0.0, (1.0 + (soil["alpha"] * np.abs(h)) ** soil["n"]) ** (-m), 1.0)
+    return soil["thetar"] + (soil["thetas"] - soil["thetar"]) * Se
 
 
 def features(Hc, hist, t, th, hb):
@@ -100,7 +111,7 @@ def log_plain_run(p, max_steps=100000, cell_stride=1, time_limit=None):
     return logs
 
 
-def samples(p, logs, cell_stride=1, min_gap=1e-9, skip=0):
+def samples(p, logs, cell_stride=1, min_gap=1e-12, skip=0):
     """(X [n, 8] float32 with 6 inputs, Y [n, 2] float32 targets) from a
     log, leaving out the first `skip` steps."""
     aint = interior_area(p)[::cell_stride]
@@ -115,7 +126,7 @@ def samples(p, logs, cell_stride=1, min_gap=1e-9, skip=0):
                 hist[:, i] = logs[n - 1 - i][1][:, 0]
         tt = [x if np.isfinite(x) else -1e30 for x in t]
         f = features(Hc, hist, tt, th, hb)
-        d = Hc - hb
+        d = theta_of(Hc, p.soilB_dict) - th
         ok = np.abs(d) > min_gap
         ok[ok] = (Q[ok] / d[ok] > 0) & (rate[ok] / d[ok] > 0)
         y1 = np.log(Q[ok] / d[ok])

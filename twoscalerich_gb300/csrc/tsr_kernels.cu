@@ -353,7 +353,8 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
         __syncthreads();
         if (D.kind == 1) {
             // learned closure: one unknown per cell (interior mean water
-            // content), inflow kQ (H_c - h(theta)), rate kT (H_c - h(theta))
+            // content theta), inflow kQ (theta_B(H_c) - theta), rate
+            // kT (theta_B(H_c) - theta)
             for (int c = warp; c < nc; c += nwarps) {
                 if (cscen[c] < 0) continue;
                 const int k = ck[c];
@@ -362,9 +363,8 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
                 if (lane == 0) {
                     const VGPar& pB = S.cell_par ? S.cell_par[k] : P.pB;
                     const double th = state_at<MODE>(u, v, mc[12], coff[c]);
-                    const double hb = vg_head(th, pB, T);
                     const double Hc = interp_at(nv, mc, mc[5], mc[6]);
-                    const double d = Hc - hb;
+                    const double d = fma(pB.dth, vg_se(Hc, pB, T), pB.thr) - th;
                     const double g = S.kappa[2 * k + 1] * d;
                     Q = S.kappa[2 * k] * d;
                     if (!finite_d(g)) atomicOr(P.flag + cscen[c], 1);
@@ -1315,7 +1315,7 @@ void launch_cell_summary(const Problem& P, const double* u, const double* g, con
 // Features of a learned cell, standardised: log(-H_c), asinh of the head
 // rates over the last 3 accepted steps [m/day], theta, log(-h(theta)).
 __device__ void closure_features(const Problem& P, const ClosureDev& C, const double* u, int k, float z[6],
-                                 int* ood, double* Hc_out, double* hb_out)
+                                 int* ood, double* Hc_out, double* dth_out)
 {
     const MicroSet& S = P.m;
     const VGPar& pB = S.cell_par ? S.cell_par[k] : P.pB;
@@ -1341,7 +1341,7 @@ __device__ void closure_features(const Problem& P, const ClosureDev& C, const do
     }
     *ood = o;
     *Hc_out = Hc;
-    *hb_out = hb;
+    *dth_out = fma(pB.dth, vg_se(Hc, pB, &d_tables), pB.thr) - th;
 }
 
 // one CTA per 128 learned cells (one thread per cell), the network on
@@ -1362,8 +1362,8 @@ __global__ void __launch_bounds__(128) k_closure_update(Problem P, const double*
     const int k = mine ? C.cells[q] : 0;
     float z[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     int ood = 0;
-    double Hc = 0.0, hb = 0.0;
-    if (mine) closure_features(P, C, u, k, z, &ood, &Hc, &hb);
+    double Hc = 0.0, dth = 0.0;
+    if (mine) closure_features(P, C, u, k, z, &ood, &Hc, &dth);
     auto x_at = [&](int, int c) -> float { return z[c]; };
     auto out = [&](int, float o1, float o2) {
         if (!mine) return;
@@ -1372,7 +1372,7 @@ __global__ void __launch_bounds__(128) k_closure_update(Problem P, const double*
         const double sc = P.cell_scale ? P.cell_scale[k] : 1.0;
         const double kQ = exp(y1);
         const double kT = exp(y2) / ((sc * sc) * C.aint[P.m.cell_tpl_full[k]]);
-        const double d = fabs(Hc - hb);
+        const double d = fabs(dth);
         int flag = ood;
         const double kQold = C.kappa[2 * k];
         // the change of kQ over the last step (from the second step of the

@@ -93,6 +93,7 @@ class Problem:
         self.keff.Keff_values = ptr(self._kv)
         self.soilA = make_soil(**soilA) if isinstance(soilA, dict) else soilA
         self.soilB = make_soil(**soilB) if isinstance(soilB, dict) else soilB
+        self.soilB_dict = dict(soilB) if isinstance(soilB, dict) else None
         self.ud = capi.UserData()
         self.ud.macro_mesh = self.macro
         self.ud.micro_mesh = self.micro
