@@ -2005,6 +2005,7 @@ extern "C" int tsr_closure_set_coef(tsr_ctx* c, const double* kappa)
     if (!c || !kappa || !c->closure) return TSR_ERR_ARG;
     CK(cudaMemcpyAsync(c->d_kappa, kappa, sizeof(double) * 2 * (size_t)c->Ne, cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    for (auto& z : c->sc) z.g0_valid = false;
     return TSR_OK;
 }
 
@@ -2059,6 +2060,7 @@ extern "C" int tsr_closure_update(tsr_ctx* c, int* n_flagged)
         return TSR_ERR_TIMEOUT;
     }
     if (n_flagged) *n_flagged = w[0];
+    c->sc[0].g0_valid = false;      // G changed with the coefficients
     return TSR_OK;
 }
 
@@ -2074,6 +2076,8 @@ extern "C" int tsr_closure_advance(tsr_ctx* c, double tend, const double* tspan,
     const bool use = c->mlp && c->nl > 0;
     if (use) {
         if ((rc = tsr_closure_update(c, &nf))) return rc;
+        // new coefficients change G: the G(u) kept from the last step is stale
+        c->sc[0].g0_valid = false;
         if (nf > 0 && c->auto_fallback) {
             std::vector<int> flags((size_t)c->Ne);
             CK(cudaMemcpy(flags.data(), c->d_flags, sizeof(int) * (size_t)c->Ne, cudaMemcpyDeviceToHost));
