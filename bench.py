@@ -638,7 +638,7 @@ def run_closure_bench(args):
         "ms_per_step": 1e3 * wc / max(sc, 1), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64 state, bf16 network", "data": "synthetic",
         "config": {"workload": "learned closure, two-scale Richards", "indicator_kind":
-                   "|dkQ| |H_c - h| <= thr * max|Q(t=0)| per step", "macro_nodes":
+                   "|dkQ| |theta_B(H_c) - theta| <= thr * max|Q(t=0)| per step, after 3 steps of history", "macro_nodes":
                    "%dx%d" % (args.n_macro, args.n_macro), "micro_nodes_per_cell":
                    "%dx%d" % (args.n_micro, args.n_micro), "cells": 2 * (args.n_macro - 1) ** 2,
                    "output_times_d": times, "indicator": args.indicator, "closure_start_d": args.closure_start,

@@ -23,8 +23,9 @@ Jacobian of EXPREM sees the exact linearisation of the closure.
 
 After every step an a-posteriori indicator compares the inflow the held
 coefficients gave with the one the network gives at the new state,
-|kQ' - kQ| |d| / max(kQ' |d|, q_floor), d = theta_B(H_c) - theta (from a
-cell's second learned step on), and flags inputs outside
+|kQ' - kQ| |d| / max(kQ' |d|, q_floor), d = theta_B(H_c) - theta (once a
+cell has the three-step head history its rate inputs need), and flags
+inputs outside
 the training range; flagged cells fall back to their micro meshes and the
 plain FP64 cell kernel for the rest of the run.
 

@@ -1375,9 +1375,10 @@ __global__ void __launch_bounds__(128) k_closure_update(Problem P, const double*
         const double d = fabs(dth);
         int flag = ood;
         const double kQold = C.kappa[2 * k];
-        // the change of kQ over the last step (from the second step of the
-        // cell on: its first step had no coefficients of its own yet)
-        if (C.hcount[k] >= 1 && kQold > 0.0) {
+        // the change of kQ over the last step, once the cell's three-step
+        // head history is complete (until then the rate inputs change by
+        // construction, not because the closure is failing)
+        if (C.hcount[k] >= 3 && kQold > 0.0) {
             const double eta = fabs(kQ - kQold) * d / fmax(kQ * d, C.qfloor);
             if (eta > C.thr) flag = 1;
         }
