@@ -1,6 +1,6 @@
 """EXPREM on the GPU against the oracle's EXPREM, through the C-ABI.
 
-The benchmark spec's bound is 1e-8 relative in h and in total water content at
+The required bound is 1e-8 relative in h and in total water content at
 every saved time.  Because G, Jv, every reduction and the host-side
 decisions follow the same operation sequence, the trajectories are in fact
 required to agree bit for bit (same steps, Krylov dimensions, FuncEvals).

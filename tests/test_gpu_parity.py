@@ -3,7 +3,7 @@
 Tolerance: the kernels evaluate the same IEEE operation sequence as the
 oracle (same table-driven log/exp, same summation orders, no contraction),
 so G, Jv and the fixed-order dot products are required to match bit for
-bit; the benchmark spec's bound (1e-12 relative for G and Jv) is checked as well.
+bit; the required bound (1e-12 relative for G and Jv) is checked as well.
 """
 import numpy as np
 import pytest
