@@ -385,13 +385,14 @@ def run_closure(p, model, times, thr=1e-3, qfloor_rel=1e-3, auto_fallback=True, 
     return rec, wall, st.NumSteps, st.FuncEvals, frac
 
 
-def training_set(time_limit=45.0, skip=3, log=print):
+def training_set(time_limit=45.0, skip=1, log=print):
     """Training data from plain runs of the CPU-runnable configuration (two
     initial heads drawn from seeds 1001-1002) and of the GPU-scale plain
     configuration at 101 x 101 macro nodes (inclusion sizes and initial
-    noise from seeds 1001-1002), each run for at most time_limit seconds;
-    the first `skip` steps of every run (the decay of the initial noise)
-    are left out.  Returns (X, Y, description)."""
+    noise from seeds 1001-1002), each run for at most time_limit seconds,
+    from step `skip` on (the early steps carry the fast decay of the initial
+    noise, whose head rates a closure run meets at its start too).  Returns
+    (X, Y, description)."""
     X, Y, desc = [], [], []
     for seed in (1001, 1002):
         q = P.config1()
