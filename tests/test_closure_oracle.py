@@ -152,3 +152,30 @@ def test_samples_features_and_targets():
     # rate features: asinh(-0.1 / 0.1) = asinh(-1) once the history exists
     last = X[-p.Ne:]
     assert np.allclose(last[:, 1:4], np.arcsinh(-1.0), atol=1e-5)
+
+
+def test_theta_of_matches_oracle_vg(orc):
+    soil = P.make_soil(**P.SOIL_B)
+    out = np.empty(3)
+    for h in (-0.05, -0.7, -4.0, -30.0, 0.0, 0.3):
+        orc.oracle_vg(C.byref(soil), 0.0, h, out.ctypes.data_as(capi.dp))
+        assert abs(closure.theta_of(h, P.SOIL_B) - out[2]) <= 1e-14
+
+
+def test_standardise_and_model_round_trip(tmp_path):
+    rng = np.random.default_rng(3)
+    X = np.zeros((500, 8), dtype=np.float32)
+    X[:, :6] = rng.normal(2.0, 3.0, (500, 6))
+    Y = rng.normal(-8.0, 0.5, (500, 2)).astype(np.float32)
+    Xs, Ys, st = closure.standardise(X, Y, margin=0.25)
+    fmu, fsd, ymu, ysd, zlo, zhi = st
+    assert np.allclose(Xs[:, :6].mean(0), 0.0, atol=1e-5) and np.allclose(Xs[:, :6].std(0), 1.0, atol=1e-4)
+    assert np.all(Xs[:, 6:] == 0.0)
+    assert np.all(Xs[:, :6].min(0) >= zlo) and np.all(Xs[:, :6].max(0) <= zhi)
+    model = closure.ClosureModel(closure.init_params(4), fmu, fsd, ymu, ysd, zlo, zhi)
+    path = str(tmp_path / "model.npz")
+    model.save(path)
+    m2 = closure.ClosureModel.load(path)
+    assert np.array_equal(m2.params, model.params)
+    assert np.array_equal(m2.norm(), model.norm()) and np.array_equal(m2.zrange(), model.zrange())
+    assert m2.norm().size == 16 and m2.zrange().size == 12
