@@ -659,10 +659,11 @@ def run_closure_bench(args):
 # FP64 instructions (DADD + DMUL + DFMA, thread level) per unknown of one
 # finite-difference Jv launch of the cell kernel, and its DRAM bytes (read +
 # write) per unknown, from the ncu capture of the 141x141 / 21x21 case in
-# profiles/k_cells_jv_141x141_21x21.md; both depend on the micro template
-# (21x21 nodes), not on the macro size, and are scaled by the unknowns.
-FP64_OPS_PER_UNKNOWN = {21: 97.13}
-G_TRAFFIC_PER_UNKNOWN = {21: 30.59}
+# profiles/k_cells_jv_141x141_21x21.md (version 5); both depend on the micro
+# template (21x21 nodes), not on the macro size, and are scaled by the
+# unknowns.
+FP64_OPS_PER_UNKNOWN = {21: 94.13}
+G_TRAFFIC_PER_UNKNOWN = {21: 30.64}
 
 
 def main():
