@@ -309,8 +309,8 @@ def run_ours(args):
     g_bytes = gbytes.value / max(gcount.value, 1)
     g_gbs = g_bytes / (g_avg_ms * 1e-3) / 1e9
     gs_gbs = sbytes.value / max(sms.value * 1e-3, 1e-30) / 1e9
-    # FP64 instructions per G from the instruction counts of the cell and
-    # macro-node kernels (ncu, per unknown) -- see the kernel profiles
+    # FP64 instructions per G from the instruction counts of the cell
+    # kernel (ncu, per unknown)
     fp64_per_unknown = FP64_OPS_PER_UNKNOWN.get(args.n_micro) if args.config == 2 else None
     fp64 = None
     if fp64_per_unknown:
@@ -658,10 +658,10 @@ def run_closure_bench(args):
 
 # FP64 instructions (DADD + DMUL + DFMA, thread level) per unknown of one
 # finite-difference Jv launch of the cell kernel, and its DRAM bytes (read +
-# write) per unknown, from the ncu capture of the 141x141 / 21x21 case in
-# profiles/k_cells_jv_141x141_21x21.md (version 5); both depend on the micro
-# template (21x21 nodes), not on the macro size, and are scaled by the
-# unknowns.
+# write) per unknown, from an ncu capture of the 141x141 / 21x21 case
+# (1629.2 M instructions and 530.3 MB for 17,307,081 unknowns); both depend
+# on the micro template (21x21 nodes), not on the macro size, and are
+# scaled by the unknowns.
 FP64_OPS_PER_UNKNOWN = {21: 94.13}
 G_TRAFFIC_PER_UNKNOWN = {21: 30.64}
 
