@@ -650,9 +650,12 @@ extern "C" int tsr_mlp_train(tsr_mlp* m, int epochs, int batch, float lr, float 
     std::vector<int> idx((size_t)n);
     for (long long i = 0; i < n; ++i) idx[(size_t)i] = (int)i;
     std::mt19937_64 rng(seed);
-    std::vector<float> lh((size_t)nb);
     float* h_loss = nullptr;
     CKM(cudaMallocHost(&h_loss, sizeof(float) * (size_t)nb));
+    struct PinnedGuard {
+        float* p;
+        ~PinnedGuard() { cudaFreeHost(p); }
+    } guard{h_loss};
     const long long total = nb * epochs;
     long long it = 0;
     for (int e = 0; e < epochs; ++e) {
@@ -662,24 +665,17 @@ extern "C" int tsr_mlp_train(tsr_mlp* m, int epochs, int batch, float lr, float 
         for (long long b = 0; b < nb; ++b, ++it) {
             k_gather<<<(batch + 255) / 256, 256, 0, m->s>>>(m->d_x, m->d_y, m->d_idx + b * batch, batch, m->b_x,
                                                             m->b_y);
-            if ((rc = grad_batch(m, batch))) {
-                cudaFreeHost(h_loss);
-                return rc;
-            }
+            if ((rc = grad_batch(m, batch))) return rc;
             CKM(cudaMemcpyAsync(h_loss + b, m->d_loss, sizeof(float), cudaMemcpyDeviceToHost, m->s));
             const double frac = (double)it / (double)std::max<long long>(total - 1, 1);
             const float lr_t = (float)(lr * (0.01 + 0.99 * 0.5 * (1.0 + std::cos(3.14159265358979 * frac))));
-            if ((rc = tsr_mlp_adamw_step(m, lr_t, wd))) {
-                cudaFreeHost(h_loss);
-                return rc;
-            }
+            if ((rc = tsr_mlp_adamw_step(m, lr_t, wd))) return rc;
         }
         CKM(cudaStreamSynchronize(m->s));
         double s = 0.0;
         for (long long b = 0; b < nb; ++b) s += h_loss[b];
         if (loss_hist) loss_hist[e] = (float)(s / (double)nb);
     }
-    cudaFreeHost(h_loss);
     return TSR_OK;
 }
 
