@@ -1855,7 +1855,16 @@ extern "C" int tsr_autotune(tsr_ctx* c, const double* u_host, int reps, double* 
     const int bud[] = {48 * 1024, 64 * 1024, 96 * 1024, 144 * 1024, 200 * 1024};
     double best = 1e30;
     int bt = c->tuned_threads, bb = c->tuned_budget;
-    cudaEvent_t e0, e1;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    struct EventGuard {
+        cudaEvent_t* a;
+        cudaEvent_t* b;
+        ~EventGuard()
+        {
+            if (*a) cudaEventDestroy(*a);
+            if (*b) cudaEventDestroy(*b);
+        }
+    } guard{&e0, &e1};
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
     for (int T : thr)
@@ -1877,8 +1886,6 @@ extern "C" int tsr_autotune(tsr_ctx* c, const double* u_host, int reps, double* 
                 bb = B;
             }
         }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     int rc = tsr::plan_cells(c, bt, bb);
     if (rc) return rc;
     if (best_ms) *best_ms = best;
