@@ -314,8 +314,8 @@ void  tsr_pinned_free(void* p);
 /* *d_out = sum_i d_x[i] * d_y[i] over n doubles, in the same fixed order as
  * tsr_dot (identical bits), without a context and without allocating device
  * memory: for callers that cannot call cudaMalloc (an embedding program that
- * owns all device memory, code running under stream capture, loops that
- * cannot afford an allocation's synchronisation).  All pointers are device
+ * owns all device memory through its own pool, loops that cannot afford an
+ * allocation's device-wide synchronisation).  All pointers are device
  * pointers; the call is asynchronous on `stream` (NULL: the default stream).
  * Its scratch is a fixed file-scope device array of 64 KB + 256 B that every
  * GPU loading the library keeps until exit, so n is limited to 67,108,864

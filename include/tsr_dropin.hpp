@@ -21,10 +21,15 @@ int Gfunc_gpu(double* g, double* u, user_data_struct user_data);
 // double& t, double tend, double* tspan, double* tspan_solns, double* u0,
 // user_data_struct user_data, exprem_options_struct options,
 // exprem_stats_struct& stats) (include/main.h:29-32).  Takes one accepted
-// step and returns, as the reference's driver loop expects.  The right-hand
-// side is always the GPU G of user_data (the Gfunc argument is accepted for
-// signature compatibility; pass Gfunc_gpu).  Returns 0, or -1 on failure
-// (the reference's fatal code, src/main.cpp:319-322).
+// step and returns, as the reference's driver loop expects.  The Gfunc
+// argument is IGNORED: the right-hand side is always the library's GPU G of
+// user_data, evaluated on the device inside the Krylov loop (a host
+// function pointer cannot be called there).  It is accepted only for
+// signature compatibility; pass Gfunc_gpu.  The device context is the one
+// registered for user_data (keyed by its macro element array, as for
+// Gfunc_gpu; tsr_set_default_ext supplies model extensions before the first
+// call).  Returns 0, or -1 on failure (the reference's fatal code,
+// src/main.cpp:319-322).
 int exprem_gpu(int (*Gfunc)(double* g, double* u, user_data_struct user_data), int N,
                double& t, double tend, double* tspan, double* tspan_solns, double* u0,
                user_data_struct user_data, exprem_options_struct options,

@@ -160,10 +160,12 @@ typedef struct tsr_model_ext {
     /* Learned closure (no counterpart in the reference): with cell_learned
      * non-NULL, cell k with cell_learned[k] = 1 carries one unknown, the
      * mean water content of its inclusion's interior nodes, instead of its
-     * micro nodes; its exchange inflow is Q = kQ (H_c - h(theta)) and its
-     * rate d theta/dt = kT (H_c - h(theta)), with H_c the macro head at the
-     * cell centre, h the inverse retention curve of material B and (kQ, kT)
-     * = closure_coef[2k], [2k+1]. */
+     * micro nodes.  The closure relaxes that water content towards the
+     * water content of material B at the macro head: the exchange inflow is
+     * Q = kQ (theta_B(H_c) - theta) and the rate is
+     * d theta/dt = kT (theta_B(H_c) - theta), with H_c the macro head at
+     * the cell centre, theta_B the retention curve of material B and
+     * (kQ, kT) = closure_coef[2k], [2k+1]. */
     const int* cell_learned;              /* [no_elements] or NULL */
     const double* closure_coef;           /* [2 * no_elements] or NULL (zeros) */
 } tsr_model_ext;

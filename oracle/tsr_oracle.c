@@ -21,7 +21,7 @@
  * The model (two-scale Richards, model_type 3, src/main.cpp:187-192) and the
  * method (Jacobian-free exponential Rosenbrock-Euler with Arnoldi) are stated
  * from the mathematics; the choices the missing sources leave open are fixed
- * in the project's design notes and here, in comments at each step.
+ * here, in comments at each step.
  *
  * Parity pinning.  phipade and the mesh preprocessing are pinned against the
  * reference's own src/phipade.cpp, src/macro_mesh_properties.cpp and

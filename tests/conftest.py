@@ -7,7 +7,6 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-REFERENCE = "/root/reference"
 
 
 def pytest_configure(config):
@@ -18,7 +17,7 @@ def pytest_configure(config):
     if not os.path.exists(B.LIB):
         B.build()
     if not os.path.exists(os.path.join(ROOT, "oracle", "libtsr_oracle.so")):
-        B.build_oracle(REFERENCE)
+        B.build_oracle()
 
 
 def gpu_available():

@@ -9,7 +9,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from tests.helpers import ROOT
+from tests.helpers import ROOT, reference_root
 from twoscalerich_gb300 import capi
 
 
@@ -75,10 +75,10 @@ def test_structs_layout_matches_header(tmp_path):
     assert _layout_probe([os.path.join(ROOT, "include", "tsr_types.h")], tmp_path) == _ctypes_layout()
 
 
-@pytest.mark.skipif(shutil.which("g++") is None or not os.path.isdir("/root/reference/include"),
+@pytest.mark.skipif(shutil.which("g++") is None or reference_root() is None,
                     reason="reference headers not present")
 def test_structs_layout_matches_reference_headers(tmp_path):
-    ref = "/root/reference/include/"
+    ref = os.path.join(reference_root(), "include") + os.sep
     heads = [ref + h for h in ("macro_mesh.h", "micro_mesh.h", "Keff.h", "soil.h", "user_data.h",
                                "exprem_options.h", "exprem_stats.h")]
     assert _layout_probe(heads, tmp_path) == _ctypes_layout()

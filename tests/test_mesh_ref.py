@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 import oracle
-from tests.helpers import REFERENCE, golden
+from tests.helpers import golden, reference_root
 from tests.golden import make_golden as MG
 from twoscalerich_gb300 import capi
 
@@ -135,7 +135,7 @@ def test_bad_element_indices_rejected():
     assert rc == 5
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE, "tests")) or oracle.load_ref() is None,
+@pytest.mark.skipif(reference_root() is None or oracle.load_ref() is None,
                     reason="reference tree / oracle/_ref not present")
 @pytest.mark.parametrize("pair", [("macro_structured_10by10.msh", "microB_unstructured_10by10.msh"),
                                   ("macro_structured_20by20.msh", "microB_unstructured_20by20.msh")])
@@ -143,7 +143,7 @@ def test_reference_fixture_meshes_live(pair):
     """The reference's own test meshes through both preprocessors."""
     ref = oracle.load_ref()
     lib = capi.load()
-    d = os.path.join(REFERENCE, "tests", "Richards_Equation")
+    d = os.path.join(reference_root(), "tests", "Richards_Equation")
     bc = np.array([1, 3, 2, 2, 2], dtype=np.int32)        # src/main.cpp:180-184
     fmac, fmic = (os.path.join(d, f).encode() for f in pair)
     Mr, Mo = capi.MacroMesh(), capi.MacroMesh()

@@ -2,14 +2,15 @@
 library's usual fixed-order dot product (tsr_dot).
 
 Some callers cannot let a library allocate device memory -- a host program
-that owns all device memory through its own pool, code that runs during
-stream capture, latency-critical loops.  tsr_dot_device_noalloc serves them
+that owns all device memory through its own pool, latency-critical loops
+that cannot afford an allocation's device-wide synchronisation.
+tsr_dot_device_noalloc serves them
 with a fixed scratch array compiled into the library instead of a context.
 This test calls it through the C-ABI on device buffers the caller owns, twice
 in a row with different data and sizes (the scratch array and its counter
 are reused across calls), and requires the same bits as tsr_dot -- the
-tolerance every reduction test in this suite uses.  The file is named so
-that pytest collects it last.
+tolerance every reduction test in this suite uses; an empty sum must give
++0.0.  The file is named so that pytest collects it last.
 """
 import ctypes as C
 
@@ -43,6 +44,18 @@ def test_noalloc_dot_matches_tsr_dot_on_two_calls():
         torch.cuda.synchronize()
         got = float(out.cpu()[0])
         assert got == expected
+
+
+def test_noalloc_dot_empty_sum_is_positive_zero():
+    torch = pytest.importorskip("torch")
+    lib = capi.load()
+    out = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    rc = lib.tsr_dot_device_noalloc(None, None, 0, C.c_void_p(out.data_ptr()), None)
+    assert rc == capi.TSR_OK, capi.last_error()
+    torch.cuda.synchronize()
+    got = float(out.cpu()[0])
+    assert got == 0.0 and np.copysign(1.0, got) == 1.0
 
 
 def test_noalloc_dot_rejects_sizes_beyond_its_scratch():

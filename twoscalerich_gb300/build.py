@@ -88,13 +88,17 @@ def build(verbose=False, force=False):
     return LIB
 
 
-def build_oracle(reference_root="/root/reference"):
+def build_oracle(reference_root=None):
     """Build the CPU oracle (always) and, when the reference tree is
-    present, the library compiled from the reference's own sources."""
+    present, the library compiled from the reference's own sources (the
+    tree is reference_root, else TSR_REFERENCE_ROOT, else the oracle
+    recipe's default)."""
     oracle_dir = os.path.join(HERE, "..", "oracle")
     _run(["make", "-s", "-C", oracle_dir, "oracle"])
-    if os.path.isdir(os.path.join(reference_root, "src")):
-        _run(["make", "-s", "-C", oracle_dir, "ref", "REF=%s" % reference_root])
+    cmd = ["make", "-s", "-C", oracle_dir, "ref-if-present"]
+    if reference_root:
+        cmd.append("REF=%s" % reference_root)
+    _run(cmd)
 
 
 if __name__ == "__main__":

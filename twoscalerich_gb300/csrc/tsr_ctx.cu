@@ -139,6 +139,10 @@ struct tsr_ctx {
     tsr_mlp* mlp = nullptr;
     ClosureDev cdev{};
     bool auto_fallback = true;
+    // set when a bounded wait of the closure network expired: its tensor
+    // memory may have been released under MMAs still in flight, so the
+    // context refuses further work (free it and build a new one)
+    bool unusable = false;
 };
 
 namespace {
@@ -842,9 +846,15 @@ int fetch_scalars(tsr_ctx* c, int slot, double* out)
     return TSR_OK;
 }
 
-// the scenario mask of the next launches (no copy when unchanged)
+// the scenario mask of the next launches (no copy when unchanged); every
+// launching path passes through here, so a context marked unusable stops
+// here before it launches anything
 int set_active(tsr_ctx* c, const std::vector<int>& on)
 {
+    if (c->unusable) {
+        set_error("context unusable after an expired tensor-core wait; free it and create a new one");
+        return TSR_ERR_TIMEOUT;
+    }
     if (c->S == 1 || on == c->active_now) return TSR_OK;
     CK(cudaStreamSynchronize(c->stream));   // the staging buffer may still be in flight
     for (int s = 0; s < c->S; ++s) c->h_active[s] = on[s];
@@ -1091,7 +1101,8 @@ extern "C" int tsr_dot(tsr_ctx* c, const double* x, const double* y, int n, doub
 
 // ---- EXPREM ------------------------------------------------------------------
 // The same algorithm, operation for operation, as the oracle's
-// oracle_exprem_step (reference src/exprem.cpp), run for the S scenarios of
+// oracle_exprem_step (the reference's exprem, include/main.h:29-32, whose body
+// is not in its tree), run for the S scenarios of
 // a context in lockstep: each launch covers the scenarios that need it (a
 // device mask), every reduction is segmented per scenario in the
 // single-problem order, and each scenario keeps its own step size, Krylov
@@ -2054,6 +2065,8 @@ extern "C" int tsr_closure_attach(tsr_ctx* c, tsr_mlp* mlp, const double* norm, 
 extern "C" int tsr_closure_update(tsr_ctx* c, int* n_flagged)
 {
     if (!c || !c->closure || !c->mlp || !c->sc[0].loaded) return TSR_ERR_ARG;
+    int rc0 = all_active(c);     // refuses an unusable context
+    if (rc0) return rc0;
     // word 0: flagged cells; word 1: a bounded wait of the network expired
     CK(cudaMemsetAsync(c->d_nflag, 0, 2 * sizeof(int), c->stream));
     ClosureDev C = closure_dev(c);
@@ -2063,7 +2076,8 @@ extern "C" int tsr_closure_update(tsr_ctx* c, int* n_flagged)
     int w[2] = {0, 0};
     CK(cudaMemcpy(w, c->d_nflag, 2 * sizeof(int), cudaMemcpyDeviceToHost));
     if (w[1]) {
-        set_error("closure update: a wait on the tensor-core barrier expired");
+        c->unusable = true;
+        set_error("closure update: a wait on the tensor-core barrier expired (context now unusable)");
         return TSR_ERR_TIMEOUT;
     }
     if (n_flagged) *n_flagged = w[0];
@@ -2188,6 +2202,12 @@ extern "C" int tsr_checkpoint_save(tsr_ctx* c, const char* path, const exprem_st
 extern "C" int tsr_checkpoint_load(tsr_ctx* c, const char* path, exprem_stats_struct* stats)
 {
     if (!c || !path || !stats) return TSR_ERR_ARG;
+    if (c->closure) {
+        // the closure's head history, coefficients and cell layout are not
+        // in the file, so a resumed closure run would not match its state
+        set_error("checkpoints of learned-closure contexts are not supported");
+        return TSR_ERR_ARG;
+    }
     FILE* f = std::fopen(path, "rb");
     if (!f) {
         set_error(std::string("cannot open ") + path);

@@ -592,7 +592,7 @@ int phipade_host(double* phiH, const double* H, double alpha, int m, int ldH, in
         double A = alpha * H[0];
         double eA = std::exp(A);
         if (eA == 1.0) {
-            phiH[0] = 1.0;                   // limit value; see DESIGN notes on phipade
+            phiH[0] = 1.0;                   // limit phi_1(A) -> 1 as A -> 0 (the reference returns 0 here)
         } else if (eA == 0.0) {
             phiH[0] = -1.0 / A;
         } else {

@@ -13,8 +13,8 @@
 //   * transcendentals are evaluated once per node, never per face;
 //   * the macro element terms ride on the CTA of the element's cell (cell k
 //     belongs to macro element k), so one G costs two launches.
-// All reductions use one fixed order (described with the oracle and in the
-// design notes); the finite-difference Jv, the Gram-Schmidt coefficients
+// All reductions use one fixed order (restated step by step in the oracle);
+// the finite-difference Jv, the Gram-Schmidt coefficients
 // and the step-error norm are therefore reproducible bit for bit.
 //
 // The code is compiled with -fmad=false: every fused multiply-add is an

@@ -380,6 +380,10 @@ struct tsr_mlp {
     int step = 0;
     cudaStream_t s = nullptr;
     int* d_err = nullptr;
+    // set when a bounded wait of the tcgen05 inference expired (its tensor
+    // memory may have been released under MMAs in flight): the network
+    // refuses further work
+    bool unusable = false;
 };
 
 namespace {
@@ -555,6 +559,10 @@ cudaStream_t mlp_stream(const tsr_mlp* m) { return m ? m->s : nullptr; }
 extern "C" int tsr_mlp_forward(tsr_mlp* m, const float* x_host, int n, float* y_host, int fused)
 {
     if (!m || !x_host || !y_host || n < 0) return TSR_ERR_ARG;
+    if (m->unusable) {
+        set_error("network unusable after an expired tensor-core wait; free it and create a new one");
+        return TSR_ERR_TIMEOUT;
+    }
     if (n == 0) return TSR_OK;
     int rc = mlp_reserve(m, n);
     if (rc) return rc;
@@ -569,7 +577,8 @@ extern "C" int tsr_mlp_forward(tsr_mlp* m, const float* x_host, int n, float* y_
         CKM(cudaMemcpyAsync(y_host, m->b_y, sizeof(float) * (size_t)n * kMlpOut, cudaMemcpyDeviceToHost, m->s));
         CKM(cudaStreamSynchronize(m->s));
         if (herr) {
-            set_error("tcgen05 inference: a wait on the MMA barrier expired");
+            m->unusable = true;
+            set_error("tcgen05 inference: a wait on the MMA barrier expired (network now unusable)");
             return TSR_ERR_TIMEOUT;
         }
         return TSR_OK;

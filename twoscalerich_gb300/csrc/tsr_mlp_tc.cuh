@@ -182,7 +182,17 @@ __device__ bool tc_forward_tile(unsigned char* sm, uint32_t tmem, const float* _
             }
         }
         phase ^= 1u;
-        if (!__syncthreads_and(ok ? 1 : 0)) return false;
+        if (!__syncthreads_and(ok ? 1 : 0)) {
+            // The wait expired: the committed MMAs may still be writing the
+            // accumulators.  Give them one more bounded wait before the
+            // caller releases the tensor memory.
+            spins = 0;
+            while (!bar_try_wait(bar, phase ^ 1u) && ++spins <= kTcSpinLimit) {
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            __syncthreads();
+            return false;
+        }
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
         // epilogue: this warp's 32 rows of D
         const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);

@@ -3,10 +3,9 @@
 //
 // Who needs it: a program that embeds this solver and owns every byte of
 // device memory through its own pool hands the library views into memory it
-// already holds, and forbids allocations behind its back; code that runs
-// while a stream is being captured into a CUDA graph may not call
-// cudaMalloc; and latency-critical loops cannot afford the device-wide
-// synchronisation a cudaMalloc/cudaFree pair can cause.  The library's
+// already holds, and forbids allocations behind its back; and latency-
+// critical loops cannot afford the device-wide synchronisation a
+// cudaMalloc/cudaFree pair can cause.  The library's
 // usual entry points keep their scratch in buffers that tsr_init allocates;
 // this one needs no context and no allocation at all.
 //
