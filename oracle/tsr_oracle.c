@@ -211,6 +211,13 @@ static double block256(double* acc)
 #define CHUNK 8192
 #define BLK 256
 
+/* Threads of the vector passes and of the chunk loop of the reductions
+ * (set from the nthreads argument of the EXPREM step).  Each chunk's
+ * partial is formed by one thread in the fixed order above and the chunk
+ * partials are combined in the fixed order, so the thread count changes
+ * the speed, never the bits. */
+static int o_threads = 1;
+
 typedef double (*term_fn)(long i, const void* ctx, double acc);
 
 static double chunked_reduce(long n, term_fn fn, const void* ctx)
@@ -218,6 +225,7 @@ static double chunked_reduce(long n, term_fn fn, const void* ctx)
     long nb = (n + CHUNK - 1) / CHUNK;
     if (nb == 0) return 0.0;
     double* P = (double*)malloc(sizeof(double) * (size_t)nb);
+#pragma omp parallel for num_threads(o_threads) schedule(static) if (nb >= 64 && o_threads > 1)
     for (long b = 0; b < nb; ++b) {
         double acc[BLK];
         for (int t = 0; t < BLK; ++t) {
@@ -719,9 +727,12 @@ int oracle_jv(oracle_problem* P, const double* u, const double* g0, const double
     long N = P->N;
     double* x = (double*)malloc(sizeof(double) * (size_t)N);
     double* gx = (double*)malloc(sizeof(double) * (size_t)N);
+    const int nt = nthreads > 1 ? nthreads : 1;
+#pragma omp parallel for num_threads(nt) schedule(static) if (nt > 1)
     for (long i = 0; i < N; ++i) x[i] = fma(eps, v[i], u[i]);
     int rc = oracle_g(P, x, gx, nthreads);
     double inv = 1.0 / eps;
+#pragma omp parallel for num_threads(nt) schedule(static) if (nt > 1)
     for (long i = 0; i < N; ++i) w[i] = (gx[i] - g0[i]) * inv;
     free(x);
     free(gx);
@@ -972,6 +983,7 @@ static int alloc_workspace(oracle_problem* P, int maxk)
 static void combine(const oracle_problem* P, const double* u, const double* c, int m, double* out)
 {
     long N = P->N;
+#pragma omp parallel for num_threads(o_threads) schedule(static) if (o_threads > 1)
     for (long l = 0; l < N; ++l) {
         double a = u[l];
         for (int i = 0; i < m; ++i) a = fma(c[i], P->V[(size_t)i * N + l], a);
@@ -988,6 +1000,7 @@ int oracle_exprem_step(oracle_problem* P, double* t_io, double tend, const doubl
     const long N = P->N;
     const int maxk = opt->MaxKrylov < (int)N ? opt->MaxKrylov : (int)N;
     if (alloc_workspace(P, maxk)) return 6;
+    o_threads = nthreads > 1 ? nthreads : 1;
     double t = *t_io;
     if (t == 0.0) {
         st->NumSteps = 0;
@@ -1018,6 +1031,7 @@ int oracle_exprem_step(oracle_problem* P, double* t_io, double tend, const doubl
     const int ldH = maxk + 1;
     memset(Hm, 0, sizeof(double) * (size_t)ldH * (size_t)maxk);
     /* weights of the error norm from the current state */
+#pragma omp parallel for num_threads(o_threads) schedule(static) if (o_threads > 1)
     for (long l = 0; l < N; ++l) P->winv[l] = 1.0 / fma(opt->RelTol, fabs(u[l]), opt->AbsTol);
     const double beta = sqrt(oracle_dot(P->g0, P->g0, N));
     const double nu = sqrt(oracle_dot(u, u, N));
@@ -1029,6 +1043,7 @@ int oracle_exprem_step(oracle_problem* P, double* t_io, double tend, const doubl
         m = 0;
     } else {
         double ib = 1.0 / beta;
+#pragma omp parallel for num_threads(o_threads) schedule(static) if (o_threads > 1)
         for (long l = 0; l < N; ++l) V[l] = P->g0[l] * ib;
         for (int j = 0; j < maxk; ++j) {
             double* vj = V + (size_t)j * N;
@@ -1040,6 +1055,7 @@ int oracle_exprem_step(oracle_problem* P, double* t_io, double tend, const doubl
                 double hij = oracle_dot(P->w, vi, N);
                 Hm[(size_t)j * ldH + i] = hij;
                 hs = fma(hij, hij, hs);
+#pragma omp parallel for num_threads(o_threads) schedule(static) if (o_threads > 1)
                 for (long l = 0; l < N; ++l) P->w[l] = fma(-hij, vi[l], P->w[l]);
             }
             double hn = sqrt(oracle_dot(P->w, P->w, N));
@@ -1051,6 +1067,7 @@ int oracle_exprem_step(oracle_problem* P, double* t_io, double tend, const doubl
             }
             double ih = 1.0 / hn;
             double* vn = V + (size_t)(j + 1) * N;
+#pragma omp parallel for num_threads(o_threads) schedule(static) if (o_threads > 1)
             for (long l = 0; l < N; ++l) vn[l] = P->w[l] * ih;
             if (m < opt->MinKrylov && m < maxk) continue;
             vnw = sqrt(oracle_wsq(vn, P->winv, N) / (double)N);
@@ -1098,6 +1115,7 @@ int oracle_exprem_step(oracle_problem* P, double* t_io, double tend, const doubl
                 z[i] = a;
             }
             double dt3 = dt / 3.0;
+#pragma omp parallel for num_threads(o_threads) schedule(static) if (o_threads > 1)
             for (long l = 0; l < N; ++l) {
                 double d = P->g1[l] - P->g0[l];
                 for (int i = 0; i < mz; ++i) d = fma(-z[i], V[(size_t)i * N + l], d);

@@ -157,3 +157,46 @@ def test_reference_fixture_meshes_live(pair):
     _compare(Mo, ref_M, MG.MACRO_FIELDS, tri=(Mo.no_verts == 3))
     _compare(mo, ref_m, MG.MICRO_FIELDS, tri=True)
     assert abs(capi.as_array(Mo.CV_area, Mo.no_nodes).sum() - 1.0) < 1e-12
+
+
+def test_reference_fixture_through_library_readers(tmp_path):
+    """The reference's own scenario (its problem_options.txt, 10x10
+    quadrilateral mesh, 167-node inclusion mesh and Keff table, kept in
+    tests/golden/ref_fixture.npz) assembled by this library's readers the
+    way the reference's main() assembles it: same geometry as the
+    reference's own preprocessing, same Keff table, and the driver's
+    boundary_flux quirk (18 values for 19 reads: boundary_flux = 1.89)."""
+    from tests.helpers import FIXTURE, write_reference_fixture
+    from twoscalerich_gb300 import problem as P
+    g = np.load(FIXTURE)
+    p = P.from_reference_files(write_reference_fixture(str(tmp_path)))
+    assert p.ud.boundary_flux == 1.89 == g["options/boundary_flux"][0]
+    assert p.u0[0] == -20.0 and p.tend == 2.0 and list(p.tspan) == [2.0, 1.0, 2.0]
+    assert p.N == 121 + 100 * 167
+    ref_M = {f: g["refgeom/macro/%s" % f] for f, _, _ in MG.MACRO_FIELDS}
+    ref_m = {f: g["refgeom/micro/%s" % f] for f, _, _ in MG.MICRO_FIELDS}
+    _compare(p.macro, ref_M, MG.MACRO_FIELDS, tri=False)
+    _compare(p.micro, ref_m, MG.MICRO_FIELDS, tri=True)
+    assert abs(p.micro.cell_area - g["refgeom/micro/cell_area"][0]) <= np.spacing(p.micro.cell_area)
+    K = p.keff
+    assert (K.epsilonA, K.no_hvalues, K.logr, K.logh_first) == (
+        g["keff/header"][0], int(g["keff/header"][1]), g["keff/header"][2], g["keff/header"][3])
+    assert np.array_equal(capi.as_array(K.Keff_values, 4 * K.no_hvalues), g["keff/values"])
+    p.close()
+
+
+def test_reference_fixture_calibration_matches_reference_writer(tmp_path):
+    """save_solution's micro-boundary calibration (src/save_solution.cpp:41-102)
+    of the reference's own scenario, on the geometry this library reads."""
+    from tests.helpers import FIXTURE, write_reference_fixture
+    from twoscalerich_gb300 import problem as P
+    g = np.load(FIXTURE)
+    p = P.from_reference_files(write_reference_fixture(str(tmp_path)))
+    u = MG.solution_state(p.N)
+    assert np.array_equal(u[:8], g["solution/u_check"])
+    capi.check(capi.load().tsr_calibrate_micro_boundary(C.byref(p.ud), None, capi.ptr(u)), "calibrate")
+    idx, ref = g["solution/index"], g["solution/value"]
+    assert np.max(np.abs(u[idx] - ref)) <= 1e-10 * np.max(np.abs(ref))
+    untouched = np.setdiff1d(np.arange(p.N), idx)
+    assert np.array_equal(u[untouched], MG.solution_state(p.N)[untouched])
+    p.close()

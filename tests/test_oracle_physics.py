@@ -138,3 +138,31 @@ def test_infiltration_increases_water_and_saved_times():
     assert log[-1][1] == p.tend
     assert np.array_equal(sol[-1], u)   # the last saved time is t_end
     assert st.FuncEvals > st.NumSteps
+
+
+@pytest.mark.parametrize("bc_south", [3, 4])
+def test_free_drainage_boundary_types(bc_south):
+    """BC types 3 (dh/dx = 0) and 4 (dh/dy = 0) on the south side
+    (src/main.cpp:175-178), no flow elsewhere, model_type 2, head linear in
+    y (h = -5 + 0.3 y) on macro and micro nodes: the macro assembly
+    conserves mass, so the storage rates sum to the south outflow,
+    -K22(h = -5) (1 + dh/dy) over the unit side, where type 4 zeroes dh/dy
+    and type 3 keeps it (dh/dx = 0 already)."""
+    p = P.fixture10(boundary_flux=0.0, macro_bc=(2, bc_south, 2, 2, 2))
+    p.ud.model_type = 2
+    o = oracle.Oracle(p)
+    xy = p.array("nodes", 2 * p.Mn)
+    u = np.full(p.N, -5.0)
+    u[:p.Mn] = -5.0 + 0.3 * xy[p.Mn:]
+    g = o.g(u)
+    lib = oracle.load()
+    cv = p.array("CV_area", p.Mn)
+    rate = 0.0
+    out = np.zeros(3)
+    for i in range(p.Mn):
+        lib.oracle_vg(C.byref(p.soilA), 1e-6, u[i], capi.ptr(out))
+        rate += p.keff.epsilonA * out[1] * cv[i] * g[i]
+    K = np.zeros(4)
+    lib.oracle_keff(C.byref(p.keff), -5.0, capi.ptr(K))
+    expect = -K[3] * (1.0 + (0.0 if bc_south == 4 else 0.3))
+    assert abs(rate - expect) <= 1e-12 * abs(expect), (rate, expect)

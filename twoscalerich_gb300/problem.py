@@ -61,12 +61,14 @@ class Problem:
         template of cell k and optional per-cell material B (list of dicts)."""
         lib = capi.load()
         self.name = name
-        self.macro = capi.MacroMesh()
-        self.micro = capi.MicroMesh()
         self._bc = np.ascontiguousarray(macro_bc, dtype=np.int32)
-        check(lib.tsr_macro_mesh_build(macro.nv, macro.n_nodes, ptr(macro.xy), macro.n_elems,
-                                       ptr(macro.elems), macro.bedges.size // 3, ptr(macro.bedges),
-                                       ptr(self._bc), C.byref(self.macro)), "tsr_macro_mesh_build")
+        if isinstance(macro, capi.MacroMesh):
+            self.macro = macro             # preprocessed by this library's reader (owned here)
+        else:
+            self.macro = capi.MacroMesh()
+            check(lib.tsr_macro_mesh_build(macro.nv, macro.n_nodes, ptr(macro.xy), macro.n_elems,
+                                           ptr(macro.elems), macro.bedges.size // 3, ptr(macro.bedges),
+                                           ptr(self._bc), C.byref(self.macro)), "tsr_macro_mesh_build")
         if templates is not None:
             micro = templates[0]
         self._tpl = None
@@ -77,20 +79,28 @@ class Problem:
                                                t.n_elems, ptr(t.elems), t.bedges.size // 3,
                                                ptr(t.bedges), C.byref(self._tpl[i])),
                       "tsr_micro_mesh_build")
-        check(lib.tsr_micro_mesh_build(micro.cell[0], micro.cell[1], micro.nv, micro.n_nodes,
-                                       ptr(micro.xy), micro.n_elems, ptr(micro.elems),
-                                       micro.bedges.size // 3, ptr(micro.bedges),
-                                       C.byref(self.micro)), "tsr_micro_mesh_build")
-        rows = np.asarray(keff_rows, dtype=np.float64)       # (n, 5): log10|h|, K11, K12, K21, K22
-        self._logh = np.ascontiguousarray(rows[:, 0])
-        self._kv = np.ascontiguousarray(rows[:, 1:].T.ravel())   # component-major
-        self.keff = capi.Keff()
-        self.keff.epsilonA = epsA
-        self.keff.no_hvalues = len(rows)
-        self.keff.logh_first = rows[0, 0] if logh_first is None else logh_first
-        self.keff.logr = (rows[1, 0] - rows[0, 0]) if logr is None else logr
-        self.keff.logh_values = ptr(self._logh)
-        self.keff.Keff_values = ptr(self._kv)
+        if isinstance(micro, capi.MicroMesh):
+            self.micro = micro
+        else:
+            self.micro = capi.MicroMesh()
+            check(lib.tsr_micro_mesh_build(micro.cell[0], micro.cell[1], micro.nv, micro.n_nodes,
+                                           ptr(micro.xy), micro.n_elems, ptr(micro.elems),
+                                           micro.bedges.size // 3, ptr(micro.bedges),
+                                           C.byref(self.micro)), "tsr_micro_mesh_build")
+        self._keff_owned = isinstance(keff_rows, capi.Keff)
+        if self._keff_owned:
+            self.keff = keff_rows          # read by this library's reader (owned here)
+        else:
+            rows = np.asarray(keff_rows, dtype=np.float64)   # (n, 5): log10|h|, K11, K12, K21, K22
+            self._logh = np.ascontiguousarray(rows[:, 0])
+            self._kv = np.ascontiguousarray(rows[:, 1:].T.ravel())   # component-major
+            self.keff = capi.Keff()
+            self.keff.epsilonA = epsA
+            self.keff.no_hvalues = len(rows)
+            self.keff.logh_first = rows[0, 0] if logh_first is None else logh_first
+            self.keff.logr = (rows[1, 0] - rows[0, 0]) if logr is None else logr
+            self.keff.logh_values = ptr(self._logh)
+            self.keff.Keff_values = ptr(self._kv)
         self.soilA = make_soil(**soilA) if isinstance(soilA, dict) else soilA
         self.soilB = make_soil(**soilB) if isinstance(soilB, dict) else soilB
         self.soilB_dict = dict(soilB) if isinstance(soilB, dict) else None
@@ -158,9 +168,9 @@ class Problem:
                 self.ext.scen_keff_scale = ptr(self._kscale)
         self.ud.N = self.N
         self.dirichlet_h = dirichlet_h
-        bce = capi.as_array(self.macro.boundary_condition_edges, macro.nv * self.Ne, np.int32)
-        el = capi.as_array(self.macro.elements, macro.nv * self.Ne, np.int32)
-        nv, Ne = macro.nv, self.Ne
+        nv, Ne = self.macro.no_verts, self.Ne
+        bce = capi.as_array(self.macro.boundary_condition_edges, nv * Ne, np.int32)
+        el = capi.as_array(self.macro.elements, nv * Ne, np.int32)
         mask = np.zeros(self.Mn, bool)
         for j in range(nv):
             d = bce[j * Ne:(j + 1) * Ne] == 5
@@ -222,6 +232,9 @@ class Problem:
                 if t.elements:
                     lib.tsr_micro_mesh_free(C.byref(t))
             self._tpl = None
+        if getattr(self, "_keff_owned", False) and self.keff.Keff_values:
+            lib.tsr_keff_free(C.byref(self.keff))
+            self._keff_owned = False
 
     def __del__(self):
         try:
@@ -381,24 +394,93 @@ def scenario_problem(ens, s):
     return p
 
 
-def fixture10(boundary_flux=0.05, jitter=0.25, seed=GENERATOR_SEED):
+def fixture10(boundary_flux=0.05, jitter=0.25, seed=GENERATOR_SEED, macro_bc=(1, 3, 2, 2, 2)):
     """The shape of the reference's test scenario: 10x10 quadrilaterals,
     influx segment x in [0, 0.4] on the top (BC 1), free drainage dh/dx = 0
     on the south side (BC 3), no flow elsewhere (src/main.cpp:180-184),
     model_type 3, a full 2x2 Keff(h) table, and an irregularly triangulated
-    inclusion of 11x11 nodes in a 0.1 m cell."""
+    inclusion of 11x11 nodes in a 0.1 m cell.  macro_bc: the BC types of the
+    tags -1 (top segment), -2 (south), -3 (east), -4 (west), -5 (rest of
+    the top)."""
     macro = meshgen.macro_unit_square(11, quads=True, segment=(0.0, 0.4))
     micro = meshgen.micro_square_inclusion(11, cell=0.1, side=0.6, jitter=jitter, seed=seed)
     logh = 1.3 - 0.0333 * np.arange(100)
     hh = 10.0 ** logh
     k11 = 0.02 / (1.0 + (0.6 * hh) ** 2.0)
     rows = np.stack([logh, k11, -0.06 * k11, -0.06 * k11, 0.87 * k11], 1)
-    p = Problem(macro, micro, rows, 0.64, SOIL_A, SOIL_B, macro_bc=[1, 3, 2, 2, 2],
+    p = Problem(macro, micro, rows, 0.64, SOIL_A, SOIL_B, macro_bc=list(macro_bc),
                 model_type=3, boundary_flux=boundary_flux, name="fixture10")
     p.options = default_options(AbsTol=1e-6, RelTol=1e-6, MaxKrylov=30)
     p.tend = 0.5
     p.tspan = np.concatenate([[5.0], np.linspace(0.1, 0.5, 5)])
     p.u0 = p.initial_state(-5.0)
+    return p
+
+
+def read_problem_options(path):
+    """problem_options.txt exactly as the reference's driver reads it
+    (src/main.cpp:32-146): the macro mesh, micro mesh and solution file
+    names, h0, tend, no_solns, the no_solns output times, material A (Ksat,
+    thetar, thetas, alpha, n), material B, boundary_flux.  A value missing
+    at the end of the file leaves the previous one in place, as the
+    reference's failed fscanf does (its own test file holds 18 values for
+    19 reads, so boundary_flux repeats material B's n)."""
+    tok = open(path).read().split()
+    if len(tok) < 3:
+        raise ValueError("%s: fewer than three file names" % path)
+    vals = tok[3:]
+    pos = 0
+    last = 0.0
+
+    def num():
+        nonlocal pos, last
+        if pos < len(vals):
+            last = float(vals[pos])
+        pos += 1
+        return last
+    h0, tend = num(), num()
+    no_solns = int(num())
+    tspan = [num() for _ in range(no_solns)]
+    soil = []
+    for _ in range(2):
+        Ks, thr, ths, al, n = (num() for _ in range(5))
+        soil.append(dict(Ksat=Ks, thetar=thr, thetas=ths, alpha=al, n=n))
+    return dict(macro_mesh_file=tok[0], micro_mesh_file=tok[1], solution_file=tok[2], h0=h0,
+                tend=tend, tspan=np.array(tspan), soilA=soil[0], soilB=soil[1],
+                boundary_flux=num())
+
+
+def from_reference_files(options_file, keff_file="Keff.txt", macro_bc=(1, 3, 2, 2, 2),
+                         model_type=3):
+    """A problem assembled as the reference's main() assembles it
+    (src/main.cpp:32-300) from its own input files, read by this library's
+    readers: problem_options.txt, the two mesh files it names and the Keff
+    table (relative paths are taken from the options file's directory, the
+    reference's working directory).  macro_bc and model_type are the values
+    main() hard-codes (src/main.cpp:180-192); options are the reference's
+    defaults (src/set_exprem_options.cpp:16-26) and u0 = h0 everywhere."""
+    import os
+    lib = capi.load()
+    o = read_problem_options(options_file)
+    d = os.path.dirname(os.path.abspath(options_file))
+    path = lambda f: f if os.path.isabs(f) else os.path.join(d, f)
+    bc = np.ascontiguousarray(macro_bc, dtype=np.int32)
+    M, m, K = capi.MacroMesh(), capi.MicroMesh(), capi.Keff()
+    check(lib.tsr_macro_mesh_properties(path(o["macro_mesh_file"]).encode(), C.byref(M), ptr(bc)),
+          "tsr_macro_mesh_properties")
+    check(lib.tsr_micro_mesh_properties(path(o["micro_mesh_file"]).encode(), C.byref(m)),
+          "tsr_micro_mesh_properties")
+    check(lib.tsr_read_effective_conductivity(path(keff_file).encode(), C.byref(K)),
+          "tsr_read_effective_conductivity")
+    p = Problem(M, m, K, K.epsilonA, o["soilA"], o["soilB"], macro_bc=list(macro_bc),
+                model_type=model_type, boundary_flux=o["boundary_flux"],
+                name=os.path.basename(path(o["macro_mesh_file"])))
+    p.options = default_options()
+    p.tend = o["tend"]
+    p.tspan = np.concatenate([[float(len(o["tspan"]))], o["tspan"]])
+    p.u0 = np.full(p.N, o["h0"])
+    p.h0 = o["h0"]
+    p.solution_file = o["solution_file"]
     return p
 
 
