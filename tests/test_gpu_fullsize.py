@@ -11,7 +11,7 @@ configurations themselves and require the same bits as the oracle:
     three accepted EXPREM steps (Krylov dimension up to 40), device-resident
     stepping as the benchmark times it;
   * 151 x 151, uneven micro meshes (N ~ 12.8 M): G and Jv;
-  * 64 scenarios of 51 x 51 x 15 x 15 (N = 72,170,944): G, Jv, and two
+  * 64 scenarios of 51 x 51 x 15 x 15 (N = 72,166,464): G, Jv, and two
     lockstep rounds, four scenarios checked against standalone oracle runs.
 
 The required bounds (1e-12 for G and Jv, 1e-8 for trajectories and water)
@@ -92,7 +92,7 @@ def test_config3_full_size_g_jv():
 
 def test_config4_full_size_g_and_two_rounds():
     ens = P.config4()                                # 64 x 51 x 51 x 15 x 15
-    assert ens.S == 64 and ens.N == 72_170_944
+    assert ens.S == 64 and ens.N == 72_166_464
     ctx = P.Context(ens)
     ctx.autotune(ens.u0, reps=1)
     orc = oracle.Oracle(ens, nthreads=THREADS)

@@ -12,8 +12,9 @@ and device that includes it:
 
   log:  1/c_i * 2^63 (unsigned), log(c_i) split into a multiple of 2^-42
         (stored as the integer log(c_i) * 2^42) and the remainder * 2^69;
-  exp:  2^(j/256) * 2^62, and 2^(j/256) as a double plus its remainder
-        (used where expm1 cancels).
+  exp:  2^(j/256) * 2^62, and 2^(j/256) * 2^126 as two 64-bit words (used
+        where expm1 cancels against 1); ln2/256 * 2^106 as two 64-bit words
+        (the fixed-point argument reduction).
 
 Run:  python gen_math_tables.py > tsr_math_tables.h
 """
@@ -42,6 +43,9 @@ def main():
     out.append("#define TSR_INV_LN10 %s  /* 1 / ln10 */" % float(1 / mpmath.log(10)).hex())
     out.append("#define TSR_LN2_D %s  /* ln2 rounded to double */" % float(ln2).hex())
     out.append("#define TSR_N_LN2_FIX54 %dULL  /* %d / ln2 * 2^54 */" % (rnd(N / ln2 * 2 ** 54), N))
+    c106 = rnd(ln2 / N * 2 ** 106)
+    out.append("#define TSR_LN2_N_FIX106_HI %dULL  /* ln2 / %d * 2^106, bits 64..127 */" % (c106 >> 64, N))
+    out.append("#define TSR_LN2_N_FIX106_LO %dULL  /* bits 0..63 */" % (c106 & (2 ** 64 - 1)))
     l42 = rnd(ln2 * 2 ** 42)
     out.append("#define TSR_LN2_HI42 %dLL  /* ln2 * 2^42, rounded */" % l42)
     out.append("#define TSR_LN2_R90 %dLL  /* (ln2 - TSR_LN2_HI42 * 2^-42) * 2^90 */"
@@ -67,13 +71,11 @@ def main():
     for j in range(N):
         out.append("  %dLL, \\" % rnd(mpmath.power(2, mpmath.mpf(j) / N) * 2 ** 62))
     out.append("}")
-    out.append("/* {2^(j/%d) rounded to double, remainder rounded to double} */" % N)
-    out.append("#define TSR_EXP_DTABLE_INIT { \\")
+    out.append("/* 2^(j/%d) * 2^126 rounded: {bits 64..127, bits 0..63} */" % N)
+    out.append("#define TSR_EXP126_TABLE_INIT { \\")
     for j in range(N):
-        v = mpmath.power(2, mpmath.mpf(j) / N)
-        hi = float(v)
-        lo = float(v - mpmath.mpf(hi))
-        out.append("  {%s, %s}, \\" % (hi.hex(), lo.hex()))
+        v = rnd(mpmath.power(2, mpmath.mpf(j) / N) * 2 ** 126)
+        out.append("  {%dULL, %dULL}, \\" % (v >> 64, v & (2 ** 64 - 1)))
     out.append("}")
     out.append("#endif")
     print("\n".join(out))
