@@ -55,6 +55,8 @@ def load(libm=False):
                                                   C.POINTER(capi.ExpremStats), C.c_int])
         for f in ("log", "exp", "expm1", "log1p"):
             _sig(lib, "oracle_math_" + f, C.c_double, [C.c_double])
+        _sig(lib, "oracle_math_log1p_unit", C.c_double, [C.c_double, dp])
+        _sig(lib, "oracle_math_div_many", None, [dp, dp, dp, C.c_long])
         _sig(lib, "oracle_vg", None, [C.POINTER(capi.Soil), C.c_double, C.c_double, dp])
         _sig(lib, "oracle_keff", None, [C.POINTER(capi.Keff), C.c_double, dp])
         _sig(lib, "oracle_dirichlet_mask", C.c_int, [vp, C.POINTER(C.c_ubyte)])

@@ -102,15 +102,17 @@ static vgpar make_vgpar(const soil_struct* s)
  * t >> 1, would otherwise cancel), and t/(1+t) = e/(1+e) or 1/(1+e). */
 static void vg_eval(double h, const vgpar* p, double* K, double* Cn, double* Cd, double* Se_out)
 {
-    if (h < 0.0) {
-        double ah = -h;
+    /* sign tests and sign flips on the bits (equal to h < 0, -h, -|nL| and
+     * nL >= 0 for every non-NaN value) */
+    if (tsr_lt0(h)) {
+        double ah = tsr_negate(h);
         double a = p->alpha * ah;
         double L = tsr_log(a, &T);
         double nL = p->n * L;
-        double e = tsr_exp(-fabs(nL), &T);
+        double e = tsr_exp(tsr_negabs(nL), &T);
         double s1;
         double lp = tsr_log1p_unit(e, &s1, &T);
-        int dry = nL >= 0.0;
+        int dry = tsr_ge0(nL);
         double l1 = dry ? nL + lp : lp;                /* log(1+t) */
         double y = dry ? -(p->m * lp) : p->m * (nL - lp);
         double X = tsr_exp(p->mh * l1, &T);           /* Se^(1/2) */
@@ -302,7 +304,7 @@ typedef struct oracle_problem {
      * tsr_model_ext.templates with a template per cell */
     int ntpl;
     const micro_mesh_struct* tpl;       /* [ntpl] */
-    double** faceD;             /* [ntpl][9*mNe]: per SCV face j of element e, D1, D2, ny */
+    double** faceH;             /* [ntpl][6*mNe]: per SCV face j of element e, D1/2, D2/2 */
     const int* cell_tpl;        /* [Ne] or NULL (all template 0) */
     long* cell_off;             /* [Ne] first unknown of cell k */
     vgpar* cell_pB;             /* [Ne] or NULL (all pB) */
@@ -398,8 +400,10 @@ oracle_problem* oracle_create(const user_data_struct* ud, const tsr_model_ext* e
     }
     /* face coefficients: (grad h) . n = D1 (h1 - h0) + D2 (h2 - h0) with
      * D_i = sfy_i ny + sfx_i nx (the gradient rows of the P1 interpolant
-     * dotted with the length-weighted face normal) */
-    P->faceD = (double**)malloc(sizeof(double*) * (size_t)P->ntpl);
+     * dotted with the length-weighted face normal), stored halved: the face
+     * conductivity is the mean of two nodal values, (K_a + K_b)/2, and the
+     * 1/2 rides on D (an exact scaling) */
+    P->faceH = (double**)malloc(sizeof(double*) * (size_t)P->ntpl);
     P->max_mn = 0;
     P->max_mNe = 0;
     for (int t = 0; t < P->ntpl; ++t) {
@@ -407,16 +411,15 @@ oracle_problem* oracle_create(const user_data_struct* ud, const tsr_model_ext* e
         const int mNe = mm->no_elements;
         if (mm->no_nodes > P->max_mn) P->max_mn = mm->no_nodes;
         if (mNe > P->max_mNe) P->max_mNe = mNe;
-        P->faceD[t] = (double*)malloc(sizeof(double) * 9 * (size_t)mNe);
+        P->faceH[t] = (double*)malloc(sizeof(double) * 6 * (size_t)mNe);
         for (int e = 0; e < mNe; ++e)
             for (int j = 0; j < 3; ++j) {
                 double nx = mm->normals[(size_t)(2 * j) * mNe + e];
                 double ny = mm->normals[(size_t)(2 * j + 1) * mNe + e];
                 for (int i = 1; i <= 2; ++i)
-                    P->faceD[t][(size_t)9 * e + 3 * j + i - 1] =
-                        fma(mm->shape_funcs[(size_t)(3 + i) * mNe + e], ny,
-                            mm->shape_funcs[(size_t)i * mNe + e] * nx);
-                P->faceD[t][(size_t)9 * e + 3 * j + 2] = ny;
+                    P->faceH[t][(size_t)6 * e + 2 * j + i - 1] =
+                        0.5 * fma(mm->shape_funcs[(size_t)(3 + i) * mNe + e], ny,
+                                  mm->shape_funcs[(size_t)i * mNe + e] * nx);
             }
     }
     const macro_mesh_struct* M = &ud->macro_mesh;
@@ -433,8 +436,8 @@ void oracle_destroy(oracle_problem* P)
 {
     if (!P) return;
     free(P->dirichlet);
-    for (int t = 0; t < P->ntpl; ++t) free(P->faceD[t]);
-    free(P->faceD);
+    for (int t = 0; t < P->ntpl; ++t) free(P->faceH[t]);
+    free(P->faceH);
     free(P->cell_off);
     free(P->cell_pB);
     free(P->node_off);
@@ -503,8 +506,8 @@ static double micro_cell(const oracle_problem* P, const double* x, int k, double
     const vgpar* pB = P->cell_pB ? &P->cell_pB[k] : &P->pB;
     const double s = P->cell_scale ? P->cell_scale[k] : 1.0;
     const double s2 = s * s;
-    double* h = scratch;
-    double* Kh = scratch + mn;
+    double* psi = scratch;
+    double* Kn = scratch + mn;
     double* Cn = scratch + 2 * mn;
     double* Cd = scratch + 3 * mn;
     double* acc = scratch + 4 * mn;
@@ -543,30 +546,34 @@ static double micro_cell(const oracle_problem* P, const double* x, int k, double
         } else {
             hl = x[off + l];
         }
-        h[l] = hl;
         double K, Se;
         vg_eval(hl, pB, &K, &Cn[l], &Cd[l], &Se);
-        Kh[l] = 0.5 * K;
+        /* total head psi = h + y, with y the node's template height scaled
+         * by s: for the P1 interpolant, grad(h + y) = grad h + e_y, so the
+         * gravity term rides on the head differences */
+        psi[l] = fma(s, m->vectors[mn + l], hl);
+        Kn[l] = K;
         acc[l] = 0.0;
     }
     const int exch = (P->ud.model_type == 3);
     for (int e = 0; e < mNe; ++e) {
         int v[3];
         for (int j = 0; j < 3; ++j) v[j] = m->elements[(size_t)j * mNe + e];
-        /* (grad h + e_y).n through the face coefficients; a cell scaled by s
-         * about the template has gradient grad/s and normals s n, so the
-         * gravity term is s ny while D is scale-free */
-        double d1 = h[v[1]] - h[v[0]];
-        double d2 = h[v[2]] - h[v[0]];
-        const double* D = P->faceD[t] + (size_t)9 * e;
+        /* (grad h + e_y).n / 2 = (grad psi).n / 2 through the halved face
+         * coefficients; a cell scaled by s about the template has gradient
+         * grad/s and normals s n, so D is scale-free and the scale enters
+         * through psi's height term only */
+        double d1 = psi[v[1]] - psi[v[0]];
+        double d2 = psi[v[2]] - psi[v[0]];
+        const double* H = P->faceH[t] + (size_t)6 * e;
         for (int j = 0; j < 3; ++j) {
             int a = v[j], b = v[(j + 1) % 3];
-            double dot = fma(D[3 * j + 1], d2, fma(D[3 * j], d1, s * D[3 * j + 2]));
+            double dot = fma(H[2 * j + 1], d2, H[2 * j] * d1);
             double Kf;
             if (P->kface == 1)
-                Kf = (dot > 0.0) ? (2.0 * Kh[b]) : (2.0 * Kh[a]);
+                Kf = tsr_gt0(dot) ? Kn[b] : Kn[a];        /* upwind: 2 K (dot/2) */
             else
-                Kf = Kh[a] + Kh[b];
+                Kf = Kn[a] + Kn[b];                       /* (K_a + K_b)/2 (2 dot/2) */
             double Pf = Kf * dot;           /* flow into SCV(a) from SCV(b) */
             acc[a] += Pf;
             acc[b] -= Pf;
@@ -582,7 +589,7 @@ static double micro_cell(const oracle_problem* P, const double* x, int k, double
                                      m->shape_funcs[(size_t)1 * mNe + e] * nbx);
                     double Db2 = fma(m->shape_funcs[(size_t)5 * mNe + e], nby,
                                      m->shape_funcs[(size_t)2 * mNe + e] * nbx);
-                    items[nitems++] = (2.0 * Kh[vv]) * fma(Db2, d2, fma(Db1, d1, s * nby));
+                    items[nitems++] = Kn[vv] * fma(Db2, d2, Db1 * d1);
                 }
             }
         }
@@ -1235,6 +1242,12 @@ double oracle_math_log(double x) { return tsr_log(x, &T); }
 double oracle_math_exp(double x) { return tsr_exp(x, &T); }
 double oracle_math_expm1(double x) { return tsr_expm1(x, &T); }
 double oracle_math_log1p(double x) { return tsr_log1p(x, &T); }
+double oracle_math_log1p_unit(double x, double* s1) { return tsr_log1p_unit(x, s1, &T); }
+/* the integer-pipe division over arrays (its test compares with IEEE a / b) */
+void oracle_math_div_many(const double* a, const double* b, double* out, long n)
+{
+    for (long i = 0; i < n; ++i) out[i] = tsr_div(a[i], b[i], &T);
+}
 
 /* VG relations, exported for their tests: out = {K, C, theta} */
 void oracle_vg(const soil_struct* s, double Ss, double h, double* out)

@@ -74,3 +74,66 @@ def test_tables_are_generated_from_mathematics():
     out = subprocess.run([sys.executable, os.path.join(d, "gen_math_tables.py")],
                          capture_output=True, text=True, check=True).stdout
     assert out == open(os.path.join(d, "tsr_math_tables.h")).read()
+
+
+def test_expm1_cancelling_range(o):
+    """|x| in [2^-8, ln2]: the result is formed in 128-bit fixed point from
+    the 2^126-scaled table and rounded once."""
+    rng = np.random.default_rng(5)
+    xs = np.concatenate([rng.uniform(-0.75, 0.75, 40000), -np.exp(rng.uniform(-5.6, -0.3, 20000)),
+                         [2.0 ** -8, -2.0 ** -8, math.log(2.0), -math.log(2.0), -0.35, 0.35]])
+    _check(o.oracle_math_expm1, math.expm1, xs)
+
+
+def test_log1p_unit_sum_is_exact_and_log_accurate(o):
+    """log1p(e) for e in [0, 1] also returns 1 + e rounded to double,
+    formed in fixed point: it must equal the FP64 sum exactly."""
+    rng = np.random.default_rng(6)
+    es = np.concatenate([rng.uniform(0, 1, 20000), np.exp(rng.uniform(-50, 0, 20000)),
+                         [0.0, 1.0, 2.0 ** -8, 2.0 ** -60, 2.0 ** -61, 2.0 ** -53, 3e-17, 5e-324]])
+    s1 = np.zeros(1)
+    worst = 0.0
+    from twoscalerich_gb300 import capi
+    for e in es:
+        r = o.oracle_math_log1p_unit(float(e), capi.ptr(s1))
+        assert s1[0] == 1.0 + float(e), e
+        worst = max(worst, ulps(r, math.log1p(float(e))))
+    assert worst <= 1.0, worst
+
+
+def _div_cases(rng, n):
+    ex = rng.integers(-300, 300, size=(2, n))
+    a = rng.uniform(1.0, 2.0, n) * np.exp2(ex[0]) * rng.choice([-1.0, 1.0], n)
+    b = rng.uniform(1.0, 2.0, n) * np.exp2(ex[1]) * rng.choice([-1.0, 1.0], n)
+    # divisors whose mantissa is near 1 (seed row 0), near 2, a power of two;
+    # equal mantissas; quotients near the ends of the normal range
+    edge_b = np.concatenate([1.0 + rng.integers(1, 2 ** 20, 2000) * 2.0 ** -52,
+                             2.0 - rng.integers(1, 2 ** 20, 2000) * 2.0 ** -52,
+                             np.exp2(rng.integers(-20, 20, 500).astype(float))])
+    edge_a = rng.uniform(1.0, 2.0, edge_b.size) * np.exp2(rng.integers(-20, 20, edge_b.size))
+    same = rng.uniform(1.0, 2.0, 1000)
+    big = np.array([1.7e308, 1e308, 2.2e-308, 3e-308, 1e-300, 5e-324, 0.0, -0.0, 1.0, 3.0])
+    bigd = np.array([0.9, 1.1, 1.5, 0.7, 1e10, 1.0, 2.0, 3.0, 3.0, 1.0])
+    a = np.concatenate([a, edge_a, same * 2.0 ** 7, big])
+    b = np.concatenate([b, edge_b, same, bigd])
+    return np.ascontiguousarray(a), np.ascontiguousarray(b)
+
+
+def test_integer_pipe_division_is_the_ieee_quotient(o):
+    """tsr_div (Newton-Raphson reciprocal and remainder correction on the
+    integer pipe) returns the correctly rounded quotient: the same bits as
+    the IEEE division a / b on every case (random exponents and signs,
+    divisor mantissas at both ends of [1, 2) and powers of two, equal
+    mantissas, quotients at the ends of the double range, zeros).  A binary
+    quotient is never exactly halfway between two doubles, so the rounding
+    decision rests on the remainder alone."""
+    from twoscalerich_gb300 import capi
+    rng = np.random.default_rng(7)
+    for _ in range(4):
+        a, b = _div_cases(rng, 500_000)
+        out = np.empty_like(a)
+        o.oracle_math_div_many(capi.ptr(a), capi.ptr(b), capi.ptr(out), a.size)
+        with np.errstate(over="ignore", under="ignore"):
+            ref = a / b
+        bad = np.nonzero(out.view(np.uint64) != ref.view(np.uint64))[0]
+        assert bad.size == 0, (a[bad[:5]], b[bad[:5]], out[bad[:5]], ref[bad[:5]])

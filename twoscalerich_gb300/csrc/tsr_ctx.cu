@@ -535,14 +535,15 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
                     ev.push_back(v[j]);
                 }
                 // face coefficients: (grad h).n_j = D1 (h1 - h0) + D2 (h2 - h0),
-                // D_i = sfy_i ny_j + sfx_i nx_j
+                // D_i = sfy_i ny_j + sfx_i nx_j, stored halved (the face
+                // conductivity is the mean of two nodal values; the 1/2 is an
+                // exact scaling)
                 for (int j = 0; j < 3; ++j) {
                     const double nx = m.normals[(size_t)(2 * j) * mNe + e];
                     const double ny = m.normals[(size_t)(2 * j + 1) * mNe + e];
                     for (int i = 1; i <= 2; ++i)
-                        eg.push_back(std::fma(m.shape_funcs[(size_t)(3 + i) * mNe + e], ny,
-                                              m.shape_funcs[(size_t)i * mNe + e] * nx));
-                    eg.push_back(ny);
+                        eg.push_back(0.5 * std::fma(m.shape_funcs[(size_t)(3 + i) * mNe + e], ny,
+                                                    m.shape_funcs[(size_t)i * mNe + e] * nx));
                 }
                 for (int j = 0; j < 3; ++j) {
                     node.push_back(v[j]);
@@ -561,7 +562,6 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
                         for (int i = 1; i <= 2; ++i)
                             bn.push_back(std::fma(m.shape_funcs[(size_t)(3 + i) * mNe + e], nby,
                                                   m.shape_funcs[(size_t)i * mNe + e] * nbx));
-                        bn.push_back(nby);
                         ++cnt;
                     }
                 }

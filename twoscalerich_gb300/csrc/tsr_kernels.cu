@@ -62,18 +62,20 @@ __device__ __forceinline__ bool finite_d(double x)
 }
 
 // ---- van Genuchten-Mualem (same operation sequence as the host oracle) ---
+// sign tests and sign flips run on the bits (tsr_lt0 / tsr_ge0 / tsr_negate /
+// tsr_negabs equal h < 0, nL >= 0, -h and -|nL| for every non-NaN value)
 __device__ __forceinline__ void vg_full(double h, const VGPar& p, const tsr_math_tables* T,
                                         double& K, double& Cn, double& Cd)
 {
-    if (h < 0.0) {
-        double ah = -h;
+    if (tsr_lt0(h)) {
+        double ah = tsr_negate(h);
         double a = p.alpha * ah;
         double L = tsr_log(a, T);
         double nL = p.n * L;
-        double e = tsr_exp(-fabs(nL), T);           // min(t, 1/t)
+        double e = tsr_exp(tsr_negabs(nL), T);      // min(t, 1/t)
         double s1;
         double lp = tsr_log1p_unit(e, &s1, T);
-        const bool dry = nL >= 0.0;
+        const bool dry = tsr_ge0(nL);
         double l1 = dry ? nL + lp : lp;             // log(1+t)
         double y = dry ? -(p.m * lp) : p.m * (nL - lp);
         double X = tsr_exp(p.mh * l1, T);
@@ -92,15 +94,15 @@ __device__ __forceinline__ void vg_full(double h, const VGPar& p, const tsr_math
 __device__ __forceinline__ void vg_storage(double h, const VGPar& p, const tsr_math_tables* T,
                                            double& Cn, double& Cd)
 {
-    if (h < 0.0) {
-        double ah = -h;
+    if (tsr_lt0(h)) {
+        double ah = tsr_negate(h);
         double a = p.alpha * ah;
         double L = tsr_log(a, T);
         double nL = p.n * L;
-        double e = tsr_exp(-fabs(nL), T);
+        double e = tsr_exp(tsr_negabs(nL), T);
         double s1;
         double lp = tsr_log1p_unit(e, &s1, T);
-        const bool dry = nL >= 0.0;
+        const bool dry = tsr_ge0(nL);
         double l1 = dry ? nL + lp : lp;
         double X = tsr_exp(p.mh * l1, T);
         double Se = X * X;
@@ -114,15 +116,15 @@ __device__ __forceinline__ void vg_storage(double h, const VGPar& p, const tsr_m
 
 __device__ __forceinline__ double vg_se(double h, const VGPar& p, const tsr_math_tables* T)
 {
-    if (!(h < 0.0)) return 1.0;
-    double ah = -h;
+    if (!tsr_lt0(h)) return 1.0;
+    double ah = tsr_negate(h);
     double a = p.alpha * ah;
     double L = tsr_log(a, T);
     double nL = p.n * L;
-    double e = tsr_exp(-fabs(nL), T);
+    double e = tsr_exp(tsr_negabs(nL), T);
     double s1;
     double lp = tsr_log1p_unit(e, &s1, T);
-    double l1 = nL >= 0.0 ? nL + lp : lp;
+    double l1 = tsr_ge0(nL) ? nL + lp : lp;
     double X = tsr_exp(p.mh * l1, T);
     return X * X;
 }
@@ -260,7 +262,7 @@ __device__ __forceinline__ void macro_element_terms(const Problem& P, int k, con
 // by the host-side autotuner).  For a bundle of nc cells with mn nodes and
 // mNe elements each, dynamic shared memory holds
 //   tables | misc [slots x 16] | cell ids / offsets [slots] |
-//   h[nc mn] | Kh[nc mn] | Cd[nc mn] | den[nc mn] | F[nc 3 mNe] | items[nc nb]
+//   psi[nc mn] | K[nc mn] | Cd[nc mn] | den[nc mn] | F[nc 3 mNe] | items[nc nb]
 // and the threads sweep the bundle's flattened node and element index
 // spaces.  Every cell still follows the single-cell operation sequence (the
 // same as the host oracle), so packing changes speed, never bits.
@@ -302,8 +304,8 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
         }
         const TplDesc D = S.tpl[t];
         const int mn = D.mn, mNe = D.mNe, nb = D.nb;
-        double* h = st;
-        double* Kh = h + nc * mn;
+        double* h = st;                              // total heads psi = h + s y
+        double* Kh = h + nc * mn;                    // nodal conductivities K(h)
         double* Cd = Kh + nc * mn;
         double* den = Cd + nc * mn;
         double* F = den + nc * mn;
@@ -318,7 +320,7 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
         const int* ebf = S.eb_first + D.ev / 3;
         const int* ebc = S.eb_count + D.ev / 3;
         const int* bvv = S.b_v + D.bitem;
-        const double* bnn = S.b_n + 3 * (long long)D.bitem;
+        const double* bnn = S.b_n + 2 * (long long)D.bitem;
         // per cell: id, first unknown, vertex heads and interpolant coefficients
         for (int c = warp; c < nc; c += nwarps) {
             const int k = S.bundle_cells[first + c];
@@ -331,6 +333,7 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
                 cscen[c] = on ? sc : -1;
                 coff[c] = S.cell_off[k];
                 mc[4] = P.cell_scale ? P.cell_scale[k] : 1.0;
+                mc[7] = mc[4] * mc[4];
                 mc[5] = M.cent[k];
                 mc[6] = M.cent[Ne + k];
                 mc[12] = eps;
@@ -399,23 +402,25 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
             } else {
                 hl = state_at<MODE>(u, v, mc[12], coff[c] + l);
             }
-            h[idx] = hl;
+            // total head: grad(h + y) = grad h + e_y for the P1 interpolant,
+            // so the gravity term rides on the head differences (y is the
+            // node's template height scaled by the cell's s)
+            h[idx] = fma(s, vec[mn + l], hl);
             double K, Cn, Cdl;
             vg_full(hl, pB, T, K, Cn, Cdl);
-            Kh[idx] = 0.5 * K;
+            Kh[idx] = K;
             Cd[idx] = Cdl;
-            den[idx] = fma(M.Ss, Cdl, Cn) * (cvm[l] * (s * s));
+            den[idx] = fma(M.Ss, Cdl, Cn) * (cvm[l] * mc[7]);
         }
         __syncthreads();
         // elements: SCV face fluxes and inclusion-boundary exchange items
         for (int idx = tid; idx < nc * mNe; idx += bs) {
             const int c = idx / mNe, e = idx - c * mNe;
             if (cscen[c] < 0) continue;
-            const double s = misc[16 * c + 4];
             const double* hc = h + c * mn;
             const double* Khc = Kh + c * mn;
             const int v0 = ev[3 * e], v1 = ev[3 * e + 1], v2 = ev[3 * e + 2];
-            const double* G = eg + 9 * (long long)e;   // per face: D1, D2, ny
+            const double* G = eg + 6 * (long long)e;   // per face: D1/2, D2/2
             const double h0 = hc[v0];
             const double d1 = hc[v1] - h0, d2 = hc[v2] - h0;
             const int vv[3] = {v0, v1, v2};
@@ -423,10 +428,10 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
 #pragma unroll
             for (int j = 0; j < 3; ++j) {
                 const int a = vv[j], bb = vv[(j + 1) % 3];
-                double dot = fma(G[3 * j + 1], d2, fma(G[3 * j], d1, s * G[3 * j + 2]));
+                const double dot = fma(G[2 * j + 1], d2, G[2 * j] * d1);   // (grad psi . n)/2
                 double Kf;
                 if (P.kface == 1)
-                    Kf = (dot > 0.0) ? (2.0 * Khc[bb]) : (2.0 * Khc[a]);
+                    Kf = tsr_gt0(dot) ? Khc[bb] : Khc[a];
                 else
                     Kf = Khc[a] + Khc[bb];
                 Fc[3 * e + j] = Kf * dot;
@@ -437,8 +442,8 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
                     const int f0 = ebf[e];
                     double* it = items + c * nb;
                     for (int q = 0; q < cnt; ++q) {
-                        const double* B = bnn + 3 * (long long)(f0 + q);   // Db1, Db2, nby
-                        it[f0 + q] = (2.0 * Khc[bvv[f0 + q]]) * fma(B[1], d2, fma(B[0], d1, s * B[2]));
+                        const double* B = bnn + 2 * (long long)(f0 + q);   // Db1, Db2
+                        it[f0 + q] = Khc[bvv[f0 + q]] * fma(B[1], d2, B[0] * d1);
                     }
                 }
             }
@@ -460,7 +465,7 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
                     const double f = Fc[ent >> 1];
                     acc = (ent & 1) ? (acc - f) : (acc + f);
                 }
-                g = (acc * Cd[idx]) / den[idx];
+                g = tsr_div(acc * Cd[idx], den[idx], T);     // IEEE quotient, integer pipe
             }
             if (!finite_d(g)) atomicOr(P.flag + cscen[c], 1);
             const long long o = coff[c] + l;
