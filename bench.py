@@ -19,8 +19,10 @@ over the timed steps.
          memory, copied in and out on every step (tsr_exprem_step).
 
 --impl reference times the CPU implementation of the same path on the host
-cores: the oracle's OpenMP form of Gfunc_parallel over the same problem (the
-reference's own Gfunc_parallel source is not in its tree).
+cores: the oracle's OpenMP form of Gfunc_parallel and its EXPREM step (C
+library log/exp) over the same workload, whose geometry the oracle's own
+mesh preprocessing builds, so that arm loads nothing of the GB300 library
+(the reference's own Gfunc_parallel and exprem sources are not in its tree).
 
 Run: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -148,14 +150,16 @@ def allsum(dist, x):
     return float(t.item())
 
 
-def make_problem(args):
+def make_problem(args, lib=None):
+    """The workload; lib: the mesh preprocessing that builds its geometry
+    (None: the GB300 library's; the CPU arm passes the oracle's)."""
     from twoscalerich_gb300 import problem as P
     if args.config == 4:
-        p = P.config4(scenarios=args.scenarios, n_macro=args.n_macro, n_micro=args.n_micro)
+        p = P.config4(scenarios=args.scenarios, n_macro=args.n_macro, n_micro=args.n_micro, lib=lib)
     elif args.config == 3:
-        p = P.config3(n_macro=args.n_macro)
+        p = P.config3(n_macro=args.n_macro, lib=lib)
     else:
-        p = P.config2(n_macro=args.n_macro, n_micro=args.n_micro)
+        p = P.config2(n_macro=args.n_macro, n_micro=args.n_micro, lib=lib)
     p.options.MaxKrylov = args.max_krylov
     return p
 
@@ -198,52 +202,107 @@ def workload(args, N):
             "parallelism": "replicas" if WORLD > 1 else "1 GPU"}
 
 
-def cpu_oracle_rate(p, n_evals, threads, min_seconds=10.0):
-    """G evaluations per second of the oracle's OpenMP Gfunc_parallel form:
-    at least n_evals evaluations and at least min_seconds of work."""
+def repo_libraries():
+    """Shared libraries of this repository mapped into the process (Linux)."""
+    found = set()
+    try:
+        with open("/proc/self/maps") as f:
+            for line in f:
+                path = line.split()[-1] if line.strip() else ""
+                if path.endswith(".so") and path.startswith(ROOT):
+                    found.add(os.path.relpath(path, ROOT))
+    except OSError:
+        return None
+    return sorted(found)
+
+
+def cpu_exprem_rate(p, u, t, stats, threads, min_seconds=10.0, min_steps=2):
+    """G evaluations per second of the oracle's OpenMP EXPREM (C-library
+    log/exp) stepping the workload on from state u at time t with the step
+    size in stats: at least min_steps accepted steps and min_seconds of work
+    (the first step evaluates G(u) once more, as any restart does)."""
     import oracle
+    from twoscalerich_gb300 import capi
     o = oracle.Oracle(p, nthreads=threads, libm=True)
-    g = np.empty(p.N)
-    o.lib.oracle_g(o.h, o._p(p.u0), o._p(g), threads)       # first-touch / warm-up
+    u = np.array(u, dtype=np.float64)
+    st = capi.ExpremStats()
+    C.memmove(C.byref(st), C.byref(stats), C.sizeof(st))
+    tspan = np.array([0.0])
+    solns = np.zeros(1)
+    ev0, n0 = st.FuncEvals, st.NumSteps
     t0 = time.perf_counter()
-    n = 0
-    while n < n_evals or time.perf_counter() - t0 < min_seconds:
-        o.lib.oracle_g(o.h, o._p(p.u0), o._p(g), threads)
-        n += 1
+    while st.NumSteps - n0 < min_steps or time.perf_counter() - t0 < min_seconds:
+        t = o.exprem_step(t, u, tspan, solns, p.options, st)
+        if t >= p.tend:
+            break
     el = time.perf_counter() - t0
     o.close()
-    return n / el, el, n
+    return (st.FuncEvals - ev0) / el, el, st.NumSteps - n0, st.FuncEvals - ev0
 
 
 def run_reference(args):
-    """CPU arm: the oracle's Gfunc_parallel form on all host cores."""
+    """CPU arm: the oracle's OpenMP EXPREM (Gfunc_parallel form, C-library
+    log/exp) on all host cores over the same workload, geometry from the
+    oracle's own mesh preprocessing.  Like the GPU arm, W untimed accepted
+    steps from t = 0, then K timed accepted steps; value = G evaluations per
+    second over the timed steps.  Ensembles (config 4): each step advances
+    the first 8 scenarios by one accepted step each."""
     if RANK != 0:
         return
-    p = make_problem(args)
-    threads = os.cpu_count() or 1
     import oracle
-    o = oracle.Oracle(p, nthreads=threads, libm=True)
-    g = np.empty(p.N)
+    from twoscalerich_gb300 import capi
+    from twoscalerich_gb300 import problem as P
+    threads = os.cpu_count() or 1
+    meshlib = oracle.MeshLib(libm=True)
+    if args.config == 4:
+        ens = make_problem(args, lib=meshlib)
+        probs = [P.scenario_problem(ens, s, lib=meshlib) for s in range(min(8, ens.S))]
+    else:
+        probs = [make_problem(args, lib=meshlib)]
+    runs = []
+    for p in probs:
+        runs.append(dict(o=oracle.Oracle(p, nthreads=threads, libm=True), p=p, u=p.u0.copy(),
+                         st=capi.ExpremStats(), t=0.0))
+    tspan = np.array([0.0])
+    solns = np.zeros(1)
+
+    def step():
+        for r in runs:
+            if r["t"] < r["p"].tend:
+                r["t"] = r["o"].exprem_step(r["t"], r["u"], tspan, solns, r["p"].options, r["st"])
     for _ in range(args.warmup):
-        o.lib.oracle_g(o.h, o._p(p.u0), o._p(g), threads)
-    times = []
+        step()
+    ev0 = sum(r["st"].FuncEvals for r in runs)
+    n0 = sum(r["st"].NumSteps for r in runs)
+    t0 = time.perf_counter()
     for _ in range(args.steps):
-        t0 = time.perf_counter()
-        o.lib.oracle_g(o.h, o._p(p.u0), o._p(g), threads)
-        times.append(time.perf_counter() - t0)
-    total = sum(times)
-    value = args.steps / total
+        step()
+    total = time.perf_counter() - t0
+    evals = sum(r["st"].FuncEvals for r in runs) - ev0
+    nsteps = sum(r["st"].NumSteps for r in runs) - n0
+    if args.config == 4:
+        metric, unit, value = ("scenario-steps/s (accepted EXPREM steps summed over scenarios per second)",
+                               "scenario-steps/s", nsteps / total)
+        sample = ("%d scenario-steps (scenarios 0-%d of the ensemble, one accepted step each per "
+                  "step, after %d warm-up steps)" % (nsteps, len(runs) - 1, args.warmup))
+    else:
+        metric, unit, value = METRIC, UNIT, evals / total
+        sample = ("%d accepted EXPREM steps (%d G evaluations) of the full workload after %d "
+                  "warm-up steps from t = 0, Krylov dimensions %s"
+                  % (nsteps, evals, args.warmup, [r["st"].CurrentKryDim for r in runs]))
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "impl": "reference", "metric": metric, "value": value, "unit": unit,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": workload(args, p.N),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "%d G evaluations of the full workload (one per step), "
-                                   "OpenMP Gfunc_parallel form with C-library log/exp"
-                                   % args.steps},
-        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "config": workload(args, probs[0].N if args.config != 4 else ens.N),
+        "cpu_baseline": {"value": value, "unit": unit, "cores": threads, "kind": "port",
+                         "sample": sample + "; the oracle's OpenMP Gfunc_parallel form and EXPREM "
+                                            "with C-library log/exp, geometry from the oracle's "
+                                            "own mesh preprocessing"},
+        "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "krylov_steps_per_s": nsteps / total,
+        "repo_libraries_loaded": repo_libraries(),
     }
     print(json.dumps(line))
 
@@ -352,10 +411,14 @@ def run_ours(args):
     cpu = None
     if RANK == 0 and WORLD == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        rate, el, n = cpu_oracle_rate(p, args.cpu_evals, threads, args.cpu_seconds)
+        u_now = np.empty(N)
+        capi.check(lib.tsr_exprem_store(h, capi.ptr(u_now)), "store")
+        rate, el, nst, nev = cpu_exprem_rate(p, u_now, te.value, st2, threads, args.cpu_seconds)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": "%d G evaluations of the full workload by the oracle's OpenMP "
-                         "Gfunc_parallel form with C-library log/exp (%.1f s)" % (n, el)}
+               "sample": "%d accepted EXPREM steps (%d G evaluations) of the full workload by the "
+                         "oracle's OpenMP EXPREM (Gfunc_parallel form, C-library log/exp), "
+                         "continuing from the GPU's state after its timed steps (%.1f s)"
+                         % (nst, nev, el)}
     traffic = G_TRAFFIC_PER_UNKNOWN.get(args.n_micro) if args.config == 2 else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": WORLD, "steps": args.steps,
@@ -674,7 +737,6 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n-macro", type=int, default=201)
     ap.add_argument("--n-micro", type=int, default=21)
-    ap.add_argument("--cpu-evals", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--max-krylov", type=int, default=None)
     ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4, 5],

@@ -56,6 +56,15 @@ def load(libm=False):
         for f in ("log", "exp", "expm1", "log1p"):
             _sig(lib, "oracle_math_" + f, C.c_double, [C.c_double])
         _sig(lib, "oracle_math_log1p_unit", C.c_double, [C.c_double, dp])
+        ip = capi.ip
+        _sig(lib, "oracle_macro_mesh_build", C.c_int,
+             [C.c_int, C.c_int, dp, C.c_int, ip, C.c_int, ip, ip, C.POINTER(capi.MacroMesh)])
+        _sig(lib, "oracle_micro_mesh_build", C.c_int,
+             [C.c_double, C.c_double, C.c_int, C.c_int, dp, C.c_int, ip, C.c_int, ip,
+              C.POINTER(capi.MicroMesh)])
+        _sig(lib, "oracle_macro_mesh_free", None, [C.POINTER(capi.MacroMesh)])
+        _sig(lib, "oracle_micro_mesh_free", None, [C.POINTER(capi.MicroMesh)])
+        _sig(lib, "oracle_set_exprem_options", C.c_int, [C.POINTER(capi.ExpremOptions)])
         _sig(lib, "oracle_math_div_many", None, [dp, dp, dp, C.c_long])
         _sig(lib, "oracle_vg", None, [C.POINTER(capi.Soil), C.c_double, C.c_double, dp])
         _sig(lib, "oracle_keff", None, [C.POINTER(capi.Keff), C.c_double, dp])
@@ -65,6 +74,24 @@ def load(libm=False):
         else:
             _o = lib
     return _om if libm else _o
+
+
+class MeshLib:
+    """The oracle's mesh preprocessing and solver defaults under the names
+    the problem builder calls (twoscalerich_gb300.problem, argument `lib`):
+    problems built with it load nothing of the GB300 library."""
+
+    def __init__(self, libm=False):
+        lib = load(libm)
+        self.tsr_macro_mesh_build = lib.oracle_macro_mesh_build
+        self.tsr_micro_mesh_build = lib.oracle_micro_mesh_build
+        self.tsr_macro_mesh_free = lib.oracle_macro_mesh_free
+        self.tsr_micro_mesh_free = lib.oracle_micro_mesh_free
+        self.tsr_set_exprem_options = lib.oracle_set_exprem_options
+
+    @staticmethod
+    def tsr_keff_free(keff):
+        raise RuntimeError("the oracle builds no Keff table from files")
 
 
 def load_ref():

@@ -39,8 +39,11 @@ def make_soil(Ksat, thetar, thetas, alpha, n):
     return s
 
 
-def default_options(**kw):
-    lib = capi.load()
+def default_options(lib=None, **kw):
+    """The reference's solver defaults (src/set_exprem_options.cpp:16-26)
+    with overrides.  lib: the library that provides tsr_set_exprem_options
+    (default: this package's)."""
+    lib = lib or capi.load()
     o = capi.ExpremOptions()
     check(lib.tsr_set_exprem_options(C.byref(o)), "tsr_set_exprem_options")
     for k, v in kw.items():
@@ -55,11 +58,15 @@ class Problem:
                  model_type=3, boundary_flux=0.0, dirichlet_h=0.0, specific_storage=1e-6,
                  kface=0, cell_scale=None, logh_first=None, logr=None, name="",
                  templates=None, cell_template=None, cell_soilB=None, scenarios=1,
-                 scen_soilA=None, scen_keff_scale=None):
+                 scen_soilA=None, scen_keff_scale=None, lib=None):
         """micro: the micro mesh of every cell; or, for the batched form,
         templates (list of micro meshes) with cell_template[k] naming the
-        template of cell k and optional per-cell material B (list of dicts)."""
-        lib = capi.load()
+        template of cell k and optional per-cell material B (list of dicts).
+        lib: the library whose mesh preprocessing builds the geometry
+        (tsr_macro_mesh_build / tsr_micro_mesh_build and their frees;
+        default: this package's)."""
+        lib = lib or capi.load()
+        self._lib = lib
         self.name = name
         self._bc = np.ascontiguousarray(macro_bc, dtype=np.int32)
         if isinstance(macro, capi.MacroMesh):
@@ -177,7 +184,7 @@ class Problem:
             mask[el[j * Ne:(j + 1) * Ne][d]] = True
             mask[el[((j + 1) % nv) * Ne:((j + 1) % nv + 1) * Ne][d]] = True
         self.dirichlet_nodes = mask
-        self.options = default_options()
+        self.options = default_options(lib)
         self.tspan = np.array([0.0])
         self.tend = 1.0
 
@@ -222,7 +229,7 @@ class Problem:
         return capi.as_array(getattr(s, name), n, dtype)
 
     def close(self):
-        lib = capi.load()
+        lib = self._lib
         if self.macro.elements:
             lib.tsr_macro_mesh_free(C.byref(self.macro))
         if self.micro.elements:
@@ -248,7 +255,7 @@ def constant_keff_rows(k=0.02):
     return [[2.0, k, 0.0, 0.0, k], [-2.0, k, 0.0, 0.0, k]]
 
 
-def config1(kface=0):
+def config1(kface=0, lib=None):
     """21x21 macro nodes (800 triangles), 11x11-node square inclusion of side
     0.5 per cell, cell = macro spacing 0.05 m; Dirichlet h = -0.1 on the top
     side, no flow elsewhere; h0 = -5; EXPREM tol 1e-6, Krylov <= 30,
@@ -257,15 +264,15 @@ def config1(kface=0):
     micro = meshgen.micro_square_inclusion(11, cell=0.05, side=0.5)
     p = Problem(macro, micro, constant_keff_rows(0.02), 0.75, SOIL_A, SOIL_B,
                 macro_bc=[5, 2, 2, 2, 2], model_type=3, dirichlet_h=-0.1, kface=kface,
-                name="config1")
-    p.options = default_options(AbsTol=1e-6, RelTol=1e-6, MaxKrylov=30)
+                name="config1", lib=lib)
+    p.options = default_options(lib, AbsTol=1e-6, RelTol=1e-6, MaxKrylov=30)
     p.tend = 1.0
     p.tspan = np.concatenate([[10.0], np.linspace(0.1, 1.0, 10)])
     p.u0 = p.initial_state(-5.0)
     return p
 
 
-def config2(n_macro=201, n_micro=21, seed=GENERATOR_SEED, eval_seed=EVAL_SEED):
+def config2(n_macro=201, n_micro=21, seed=GENERATOR_SEED, eval_seed=EVAL_SEED, lib=None):
     """GPU-scale plain method: n_macro^2 macro nodes, n_micro^2 micro nodes
     per cell, inclusion side per cell U(0.3, 0.7) of the cell (a per-cell
     scale of the side-0.5 template), Dirichlet h = -0.1 on the top strip
@@ -280,8 +287,8 @@ def config2(n_macro=201, n_micro=21, seed=GENERATOR_SEED, eval_seed=EVAL_SEED):
     epsA = 1.0 - (0.7 ** 3 - 0.3 ** 3) / (3 * 0.4)           # 1 - E[side^2]
     p = Problem(macro, micro, constant_keff_rows(0.02), epsA, SOIL_A, SOIL_B,
                 macro_bc=[5, 2, 2, 2, 2], model_type=3, dirichlet_h=-0.1, cell_scale=scale,
-                name="config2_%d_%d" % (n_macro, n_micro))
-    p.options = default_options(AbsTol=1e-6, RelTol=1e-6, MaxKrylov=40)
+                name="config2_%d_%d" % (n_macro, n_micro), lib=lib)
+    p.options = default_options(lib, AbsTol=1e-6, RelTol=1e-6, MaxKrylov=40)
     p.tend = 2.0
     p.tspan = np.concatenate([[10.0], np.linspace(0.2, 2.0, 10)])
     p.u0 = p.initial_state(-5.0, noise=0.1, seed=eval_seed)
@@ -292,7 +299,7 @@ MICRO_SIDES = (5, 9, 15, 21, 31, 41)
 MICRO_SIDE_P = (0.30, 0.25, 0.20, 0.12, 0.08, 0.05)
 
 
-def config3(n_macro=151, seed=GENERATOR_SEED, eval_seed=EVAL_SEED):
+def config3(n_macro=151, seed=GENERATOR_SEED, eval_seed=EVAL_SEED, lib=None):
     """Batched form with uneven micro meshes: n_macro^2 macro nodes; per cell
     a micro mesh side from {5,9,15,21,31,41} (p = .30,.25,.20,.12,.08,.05), a
     square or disk inclusion (p = 0.5) of size U(0.2, 0.8) of the cell, and
@@ -320,8 +327,8 @@ def config3(n_macro=151, seed=GENERATOR_SEED, eval_seed=EVAL_SEED):
     p = Problem(macro, None, constant_keff_rows(0.02), 1.0 - frac.mean(), SOIL_A, SOIL_B,
                 macro_bc=[5, 2, 2, 2, 2], model_type=3, dirichlet_h=-0.1, cell_scale=scale,
                 templates=templates, cell_template=tpl, cell_soilB=soils,
-                name="config3_%d" % n_macro)
-    p.options = default_options(AbsTol=1e-6, RelTol=1e-6, MaxKrylov=30)
+                name="config3_%d" % n_macro, lib=lib)
+    p.options = default_options(lib, AbsTol=1e-6, RelTol=1e-6, MaxKrylov=30)
     p.tend = 1.0
     p.tspan = np.concatenate([[10.0], np.linspace(0.1, 1.0, 10)])
     p.u0 = p.initial_state(-5.0, noise=0.1, seed=eval_seed)
@@ -339,7 +346,8 @@ def union_mesh(mesh, copies):
     return meshgen.Mesh(nv, xy, el, bed.ravel())
 
 
-def config4(scenarios=64, n_macro=51, n_micro=15, seed=GENERATOR_SEED, eval_seed=EVAL_SEED):
+def config4(scenarios=64, n_macro=51, n_micro=15, seed=GENERATOR_SEED, eval_seed=EVAL_SEED,
+            lib=None):
     """Ensemble: `scenarios` independent problems solved together, each on an
     n_macro^2 macro grid with n_micro^2 micro meshes (square inclusion of
     side 0.5), Dirichlet top h = -0.1, no flow elsewhere.  Per scenario:
@@ -364,8 +372,8 @@ def config4(scenarios=64, n_macro=51, n_micro=15, seed=GENERATOR_SEED, eval_seed
     p = Problem(macro, micro, constant_keff_rows(0.02), 0.75, SOIL_A, SOIL_B,
                 macro_bc=[5, 2, 2, 2, 2], model_type=3, dirichlet_h=-0.1, cell_soilB=cellB,
                 scenarios=scenarios, scen_soilA=soilsA, scen_keff_scale=ksA / 0.054,
-                name="config4_%dx%d_%d" % (scenarios, n_macro, n_micro))
-    p.options = default_options(AbsTol=1e-6, RelTol=1e-6, MaxKrylov=30)
+                name="config4_%dx%d_%d" % (scenarios, n_macro, n_micro), lib=lib)
+    p.options = default_options(lib, AbsTol=1e-6, RelTol=1e-6, MaxKrylov=30)
     p.tend = 1.0
     p.tspan = np.array([0.0])
     p.h0 = h0
@@ -374,7 +382,7 @@ def config4(scenarios=64, n_macro=51, n_micro=15, seed=GENERATOR_SEED, eval_seed
     return p
 
 
-def scenario_problem(ens, s):
+def scenario_problem(ens, s, lib=None):
     """Scenario s of an ensemble as a standalone problem (same unknowns)."""
     pr = ens.scenario_params
     n_macro = int(round(np.sqrt(ens.Mn // ens.S)))
@@ -386,7 +394,7 @@ def scenario_problem(ens, s):
     p = Problem(macro, micro, K, 0.75, dict(SOIL_A, Ksat=pr["Ks_A"][s], alpha=pr["alpha_A"][s],
                                             n=pr["n_A"][s]),
                 dict(SOIL_B, Ksat=pr["Ks_B"][s]), macro_bc=[5, 2, 2, 2, 2], model_type=3,
-                dirichlet_h=-0.1, name="scenario%d" % s)
+                dirichlet_h=-0.1, name="scenario%d" % s, lib=lib)
     p.options = ens.options
     p.tend = ens.tend
     p.tspan = np.array([0.0])
@@ -394,7 +402,7 @@ def scenario_problem(ens, s):
     return p
 
 
-def fixture10(boundary_flux=0.05, jitter=0.25, seed=GENERATOR_SEED, macro_bc=(1, 3, 2, 2, 2)):
+def fixture10(boundary_flux=0.05, jitter=0.25, seed=GENERATOR_SEED, macro_bc=(1, 3, 2, 2, 2), lib=None):
     """The shape of the reference's test scenario: 10x10 quadrilaterals,
     influx segment x in [0, 0.4] on the top (BC 1), free drainage dh/dx = 0
     on the south side (BC 3), no flow elsewhere (src/main.cpp:180-184),
@@ -409,8 +417,8 @@ def fixture10(boundary_flux=0.05, jitter=0.25, seed=GENERATOR_SEED, macro_bc=(1,
     k11 = 0.02 / (1.0 + (0.6 * hh) ** 2.0)
     rows = np.stack([logh, k11, -0.06 * k11, -0.06 * k11, 0.87 * k11], 1)
     p = Problem(macro, micro, rows, 0.64, SOIL_A, SOIL_B, macro_bc=list(macro_bc),
-                model_type=3, boundary_flux=boundary_flux, name="fixture10")
-    p.options = default_options(AbsTol=1e-6, RelTol=1e-6, MaxKrylov=30)
+                model_type=3, boundary_flux=boundary_flux, name="fixture10", lib=lib)
+    p.options = default_options(lib, AbsTol=1e-6, RelTol=1e-6, MaxKrylov=30)
     p.tend = 0.5
     p.tspan = np.concatenate([[5.0], np.linspace(0.1, 0.5, 5)])
     p.u0 = p.initial_state(-5.0)
