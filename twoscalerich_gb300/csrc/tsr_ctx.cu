@@ -512,7 +512,7 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
     MicroSet& S = P.m;
     S.ntpl = ntpl;
     {
-        std::vector<int> ev, cptr, cent, bnode, ebf, ebc, bv;
+        std::vector<int> ev, cptr, cent, bnode, be, bv, bl;
         std::vector<double> eg, cv, vec, bn;
         c->tpl_host.clear();
         for (int t = 0; t < ntpl; ++t) {
@@ -551,31 +551,33 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
                     node.push_back(v[(j + 1) % 3]);
                     code.push_back(((3 * e + j) << 1) | 1);
                 }
-                ebf.push_back((int)bv.size() - d.bitem);
-                int cnt = 0;
+                // inclusion-boundary items in assembly order (element,
+                // edge, half), each with its element and vertex
                 for (int j = 0; j < 3; ++j) {
                     if (m.boundary_edges[(size_t)j * mNe + e] != 1) continue;
                     for (int sh = 0; sh < 2; ++sh) {
+                        be.push_back(e);
                         bv.push_back(v[(j + sh) % 3]);
                         const double nbx = m.boundary_edge_normals[(size_t)(4 * j + 2 * sh) * mNe + e];
                         const double nby = m.boundary_edge_normals[(size_t)(4 * j + 2 * sh + 1) * mNe + e];
                         for (int i = 1; i <= 2; ++i)
                             bn.push_back(std::fma(m.shape_funcs[(size_t)(3 + i) * mNe + e], nby,
                                                   m.shape_funcs[(size_t)i * mNe + e] * nbx));
-                        ++cnt;
                     }
                 }
-                ebc.push_back(cnt);
             }
             d.nb = (int)bv.size() - d.bitem;
             d.state = 4 * mn + 3 * mNe + d.nb;
             Csr csr = group_events(mn, node, code);
             cptr.insert(cptr.end(), csr.ptr.begin(), csr.ptr.end());
             cent.insert(cent.end(), csr.ent.begin(), csr.ent.end());
+            d.bnl = (int)bl.size();
             for (int l = 0; l < mn; ++l) {
                 bnode.push_back(m.boundary_nodes[l]);
                 cv.push_back(m.CV_area[l]);
+                if (m.boundary_nodes[l] != 0) bl.push_back(l);
             }
+            d.nbn = (int)bl.size() - d.bnl;
             for (int l = 0; l < 2 * mn; ++l) vec.push_back(m.vectors[l]);
             c->tpl_host.push_back(d);
         }
@@ -602,10 +604,11 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
         if ((rc = upload(c, cptr.data(), cptr.size(), &S.csr_ptr))) return rc;
         if ((rc = upload(c, cent.data(), cent.size(), &S.csr_ent))) return rc;
         if ((rc = upload(c, bnode.data(), bnode.size(), &S.bnode))) return rc;
+        if (bl.empty()) bl.push_back(0);
+        if ((rc = upload(c, bl.data(), bl.size(), &S.bnl))) return rc;
         if ((rc = upload(c, cv.data(), cv.size(), &S.cv))) return rc;
         if ((rc = upload(c, vec.data(), vec.size(), &S.vec))) return rc;
-        if ((rc = upload(c, ebf.data(), ebf.size(), &S.eb_first))) return rc;
-        if ((rc = upload(c, ebc.data(), ebc.size(), &S.eb_count))) return rc;
+        if ((rc = upload(c, be.data(), be.size(), &S.b_e))) return rc;
         if ((rc = upload(c, bv.data(), bv.size(), &S.b_v))) return rc;
         if ((rc = upload(c, bn.data(), bn.size(), &S.b_n))) return rc;
         void* q;

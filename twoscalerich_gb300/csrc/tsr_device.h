@@ -28,7 +28,7 @@ struct TplDesc {
     int mn, mNe, nb, state;      // nodes, elements, boundary items, shared doubles per cell
     int ev, eg, csr_ptr, csr_ent, node, bitem;   // offsets (elements, nodes, items)
     int kind;                    // 0 micro mesh, 1 learned closure (one unknown per cell)
-    int pad;
+    int nbn, bnl;                // inclusion-boundary nodes: count, offset into MicroSet::bnl
 };
 
 struct MicroSet {
@@ -38,16 +38,16 @@ struct MicroSet {
     int pad;
     const TplDesc* tpl;          // [ntpl]
     const int* ev;               // 3 per element: vertices
-    const double* eg;            // 9 per element: per face j D1, D2, ny
+    const double* eg;            // 6 per element: per face j D1/2, D2/2
     const int* csr_ptr;          // mn+1 per template
     const int* csr_ent;          // (3e+j)<<1 | (1 if subtracted)
     const int* bnode;            // per node: 1 on the inclusion boundary
+    const int* bnl;              // per template: its boundary nodes (template-local indices)
     const double* cv;            // per node: CV area
     const double* vec;           // 2 per node (x then y, per template block)
-    const int* eb_first;         // per element: first boundary item (template-local)
-    const int* eb_count;         // per element
+    const int* b_e;              // per item: element (template-local)
     const int* b_v;              // per item: node (template-local)
-    const double* b_n;           // 3 per item: D1, D2, ny of the outward normal
+    const double* b_n;           // 2 per item: D1, D2 of the outward normal
     const long long* cell_off;   // [Ne] first unknown of cell k
     const int* cell_tpl;         // [Ne]
     const struct VGPar* cell_par;   // [Ne] or nullptr (all pB)

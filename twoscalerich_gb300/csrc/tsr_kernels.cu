@@ -317,8 +317,7 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
         const int* bnode = S.bnode + D.node;
         const double* cvm = S.cv + D.node;
         const double* vec = S.vec + 2 * D.node;
-        const int* ebf = S.eb_first + D.ev / 3;
-        const int* ebc = S.eb_count + D.ev / 3;
+        const int* bee = S.b_e + D.bitem;
         const int* bvv = S.b_v + D.bitem;
         const double* bnn = S.b_n + 2 * (long long)D.bitem;
         // per cell: id, first unknown, vertex heads and interpolant coefficients
@@ -351,6 +350,23 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
                 for (int i = 1; i < nv; ++i)
                     a = fma(M.sf[(long long)(m * nv + i) * Ne + k], mc[8 + i], a);
                 mc[m] = a;
+            }
+            __syncwarp();
+            // heads of the inclusion-boundary nodes: the macro interpolant at
+            // centroid + s vectors (model_type 1: at the centroid), one lane
+            // per boundary node (dense; the node loop below only reads them)
+            if (on && D.kind == 0) {
+                const int* bl = S.bnl + D.bnl;
+                const double s = mc[4];
+                for (int q = lane; q < D.nbn; q += 32) {
+                    const int l = bl[q];
+                    double px = mc[5], py = mc[6];
+                    if (M.model_type != 1) {
+                        px = fma(s, vec[l], mc[5]);
+                        py = fma(s, vec[mn + l], mc[6]);
+                    }
+                    h[c * mn + l] = interp_at(nv, mc, px, py);
+                }
             }
         }
         __syncthreads();
@@ -391,17 +407,8 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
             const double s = mc[4];
             const VGPar& pB = S.cell_par ? S.cell_par[ck[c]] : P.pB;
             const bool bnd = bnode[l] != 0;
-            double hl;
-            if (bnd) {
-                double px = mc[5], py = mc[6];
-                if (M.model_type != 1) {
-                    px = fma(s, vec[l], mc[5]);
-                    py = fma(s, vec[mn + l], mc[6]);
-                }
-                hl = interp_at(nv, mc, px, py);
-            } else {
-                hl = state_at<MODE>(u, v, mc[12], coff[c] + l);
-            }
+            // boundary heads come from the per-cell pass above
+            const double hl = bnd ? h[idx] : state_at<MODE>(u, v, mc[12], coff[c] + l);
             // total head: grad(h + y) = grad h + e_y for the P1 interpolant,
             // so the gravity term rides on the head differences (y is the
             // node's template height scaled by the cell's s)
@@ -436,16 +443,20 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
                     Kf = Khc[a] + Khc[bb];
                 Fc[3 * e + j] = Kf * dot;
             }
-            if (exch) {
-                const int cnt = ebc[e];
-                if (cnt > 0) {
-                    const int f0 = ebf[e];
-                    double* it = items + c * nb;
-                    for (int q = 0; q < cnt; ++q) {
-                        const double* B = bnn + 2 * (long long)(f0 + q);   // Db1, Db2
-                        it[f0 + q] = Khc[bvv[f0 + q]] * fma(B[1], d2, B[0] * d1);
-                    }
-                }
+        }
+        // inclusion-boundary exchange items, a dense loop of their own (as
+        // part of the element loop they left most lanes of a warp idle):
+        // K at the item's vertex times (grad psi . n_b) of its element
+        if (exch) {
+            for (int idx = tid; idx < nc * nb; idx += bs) {
+                const int c = idx / nb, q = idx - c * nb;
+                if (cscen[c] < 0) continue;
+                const double* hc = h + c * mn;
+                const int e = bee[q];
+                const double h0 = hc[ev[3 * e]];
+                const double d1 = hc[ev[3 * e + 1]] - h0, d2 = hc[ev[3 * e + 2]] - h0;
+                const double* B = bnn + 2 * (long long)q;   // Db1, Db2
+                items[idx] = Kh[c * mn + bvv[q]] * fma(B[1], d2, B[0] * d1);
             }
         }
         __syncthreads();
@@ -461,9 +472,11 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
                 double acc = 0.0;
                 const int p1 = cptr[l + 1];
                 for (int p = cptr[l]; p < p1; ++p) {
+                    // acc - f is acc + (-f): the sign flip is a bit operation,
+                    // so every entry costs one FP64 addition
                     const int ent = cent[p];
                     const double f = Fc[ent >> 1];
-                    acc = (ent & 1) ? (acc - f) : (acc + f);
+                    acc = acc + tsr_u2d(tsr_d2u(f) ^ ((uint64_t)(ent & 1) << 63));
                 }
                 g = tsr_div(acc * Cd[idx], den[idx], T);     // IEEE quotient, integer pipe
             }
@@ -520,7 +533,7 @@ __global__ void __launch_bounds__(128) k_macro_nodes(Problem P, const double* __
         for (int p = M.csr_ptr[i]; p < p1; ++p) {
             const int ent = M.csr_ent[p];
             const double c = P.contrib[ent >> 1];
-            acc = (ent & 1) ? (acc - c) : (acc + c);
+            acc = acc + tsr_u2d(tsr_d2u(c) ^ ((uint64_t)(ent & 1) << 63));
         }
         double Cn, Cd;
         vg_storage(H, M.scen_pA ? M.scen_pA[sc] : P.pA, &T, Cn, Cd);
