@@ -19,6 +19,7 @@
 //
 // The code is compiled with -fmad=false: every fused multiply-add is an
 // explicit fma(), matching the host evaluation operation for operation.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -999,6 +1000,118 @@ __global__ void __launch_bounds__(kRedThreads) k_gs_fused(SegInfo g, GsArgs A)
     }
 }
 
+// The Gram-Schmidt block for problems of at most 16 chunks (one thread-block
+// cluster, one chunk per CTA).  The passes and their arithmetic are those of
+// k_gs_fused, in the same order (same bits), but: each thread keeps its 32
+// items of w in registers for the whole block and writes w back once; the
+// basis vector of the next pass is loaded into registers before the barrier,
+// so its latency overlaps the wait, and the current one sits in the thread's
+// own slots of 64 KB of shared memory; the chunk partials go through distributed shared
+// memory instead of global memory, and every warp forms the segment totals
+// itself (at most 16 partials), so a pass costs one CTA barrier and one
+// cluster barrier.  Every CTA executes every cluster barrier, including a
+// last one after the final reads of its peers' shared memory.
+__global__ void __launch_bounds__(kRedThreads, 1) k_gs_cluster(SegInfo g, GsArgs A)
+{
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    constexpr int Q = kRedChunk / kRedThreads;      // items per thread
+    __shared__ double ws[8];
+    __shared__ double mypart[2];                    // chunk partial, by pass parity
+    extern __shared__ double vsm[];                 // [Q][kRedThreads]: basis vector of this pass
+    double* vc = vsm + threadIdx.x;                 // item q of this thread at vc[q * kRedThreads]
+    const int j = A.j;
+    const int b = (int)blockIdx.x;                  // chunk = cluster rank
+    const int lane = threadIdx.x & 31;
+    const SegBlock B = seg_block_at(g, b);
+    const bool act = !(g.active && !g.active[B.s]);
+    const long long base = B.lo + (long long)B.lb * kRedChunk + threadIdx.x;
+    const long long so = (long long)B.s * A.stride;
+    const bool writer = (b == B.b0) && threadIdx.x == 0;
+    double w[Q], vn[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const long long i = base + (long long)q * kRedThreads;
+        const bool in = act && i < B.hi;
+        w[q] = in ? A.w[i] : 0.0;
+        vc[q * kRedThreads] = in ? A.V[i] : 0.0;
+        vn[q] = (in && j >= 1) ? A.V[(size_t)A.ldV + i] : 0.0;
+    }
+    // total of the previous pass's chunk partials of this chunk's segment,
+    // formed as segment_total forms it (thread t: 0 + P[t]; block tree with
+    // the seven all-zero warps)
+    auto seg_total = [&](int par) -> double {
+        double a = 0.0;
+        if (lane < B.nb) a = 0.0 + *cl.map_shared_rank(&mypart[par], (unsigned)(B.b0 + lane));
+#pragma unroll
+        for (int d = 16; d >= 1; d >>= 1) a = a + __shfl_xor_sync(0xffffffffu, a, d);
+        const double z = 0.0;
+        return ((a + z) + (z + z)) + ((z + z) + (z + z));
+    };
+    for (int p = 0; p <= j + 2; ++p) {
+        double a = 0.0;
+        if (p == 0) {
+#pragma unroll
+            for (int q = 0; q < Q; ++q)
+                if (base + (long long)q * kRedThreads < B.hi) a = fma(w[q], vc[q * kRedThreads], a);
+        } else {
+            const double h = seg_total((p + 1) & 1);
+            if (p <= j + 1) {
+                // h = H(p-1, j); w -= h v_{p-1}; dot with v_p (or with w after the last)
+                if (writer && act) A.Hc[so + p - 1] = h;
+#pragma unroll
+                for (int q = 0; q < Q; ++q) {
+                    if (base + (long long)q * kRedThreads >= B.hi) continue;
+                    const double wn = fma(-h, vc[q * kRedThreads], w[q]);
+                    w[q] = wn;
+                    a = fma(wn, (p <= j) ? vn[q] : wn, a);
+                }
+            } else {
+                // h = ||w||^2: H(j+1, j) = sqrt, v_{j+1} = w / H(j+1, j), weighted norm
+                const double hn = sqrt(h);
+                const double ih = 1.0 / hn;
+                if (writer && act) {
+                    A.hsq[so] = h;
+                    A.Hc[so + j + 1] = hn;
+                    A.ih[so] = ih;
+                }
+                double* v = A.V + (size_t)(j + 1) * A.ldV;
+#pragma unroll
+                for (int q = 0; q < Q; ++q) {
+                    const long long i = base + (long long)q * kRedThreads;
+                    if (!act || i >= B.hi) continue;
+                    const double vv = w[q] * ih;
+                    v[i] = vv;
+                    const double rr = vv * vn[q];        // vn holds winv here
+                    a = fma(rr, rr, a);
+                }
+            }
+        }
+        const double r = block_sum_256(a, ws);
+        if (threadIdx.x == 0) mypart[p & 1] = r;
+        if (p >= 1) {
+            // the next pass's vector: v_{p+1}, or the weights for the scaling pass
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                const long long i = base + (long long)q * kRedThreads;
+                const bool in = act && i < B.hi;
+                vc[q * kRedThreads] = vn[q];
+                if (p + 1 <= j) vn[q] = in ? A.V[(size_t)(p + 1) * A.ldV + i] : 0.0;
+                else if (p + 1 == j + 2) vn[q] = in ? A.winv[i] : 0.0;
+            }
+        }
+        cl.sync();
+    }
+    // the weighted norm of v_{j+1} (total of the last pass), and w
+    if (writer && act) A.sv[so] = seg_total((j + 2) & 1);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const long long i = base + (long long)q * kRedThreads;
+        if (act && i < B.hi) A.w[i] = w[q];
+    }
+    cl.sync();        // peers may still read this CTA's partials
+}
+
 // Failure-path probe of the bounded grid barrier: CTA 1 leaves without
 // arriving, so CTA 0's wait must run out and raise *err.
 __global__ void k_barrier_probe(unsigned int* bar, int* err)
@@ -1030,7 +1143,8 @@ int barrier_probe(int* timed_out)
 }
 
 static constexpr int kGsMaxCluster = 16;
-static int g_gs_cluster_max = 0;    // largest cluster the device schedules for the fused kernel
+static constexpr int kGsClusterSmem = kRedChunk * (int)sizeof(double);   // one chunk of a vector
+static int g_gs_cluster_max = 0;    // largest cluster the device schedules for the cluster kernel
 
 int gs_fused_grid(int nsm)
 {
@@ -1040,12 +1154,16 @@ int gs_fused_grid(int nsm)
     // clusters of more than 8 CTAs are a non-portable size: use them only if
     // the device can schedule one
     g_gs_cluster_max = 0;
-    if (cudaFuncSetAttribute(k_gs_fused<true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+    if (cudaFuncSetAttribute(k_gs_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
         cudaGetLastError();
+    if (cudaFuncSetAttribute(k_gs_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, kGsClusterSmem) !=
+        cudaSuccess)
+        return occ * nsm;       // no cluster variant
     for (int cs : {kGsMaxCluster, 8}) {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3((unsigned)cs);
         cfg.blockDim = dim3(kRedThreads);
+        cfg.dynamicSmemBytes = kGsClusterSmem;
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeClusterDimension;
         attr[0].val.clusterDim.x = (unsigned)cs;
@@ -1054,7 +1172,7 @@ int gs_fused_grid(int nsm)
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         int nc = 0;
-        if (cudaOccupancyMaxActiveClusters(&nc, k_gs_fused<true>, &cfg) == cudaSuccess && nc > 0) {
+        if (cudaOccupancyMaxActiveClusters(&nc, k_gs_cluster, &cfg) == cudaSuccess && nc > 0) {
             g_gs_cluster_max = cs;
             break;
         }
@@ -1075,12 +1193,14 @@ cudaError_t launch_gs_fused(const SegInfo& g, const GsArgs& A, int max_grid, cud
     cudaLaunchAttribute attr[1];
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if (grid <= g_gs_cluster_max) {
+    if (grid <= g_gs_cluster_max && grid == g.nblocks) {
+        // one chunk per CTA, the whole grid one cluster
         attr[0].id = cudaLaunchAttributeClusterDimension;
         attr[0].val.clusterDim.x = (unsigned)grid;
         attr[0].val.clusterDim.y = 1;
         attr[0].val.clusterDim.z = 1;
-        return cudaLaunchKernelEx(&cfg, k_gs_fused<true>, g, A);
+        cfg.dynamicSmemBytes = kGsClusterSmem;
+        return cudaLaunchKernelEx(&cfg, k_gs_cluster, g, A);
     }
     attr[0].id = cudaLaunchAttributeCooperative;
     attr[0].val.cooperative = 1;
