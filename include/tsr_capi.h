@@ -86,6 +86,16 @@ void tsr_keff_free(Keff_struct* keff);
 int tsr_calibrate_micro_boundary(const user_data_struct* user_data,
                                  const tsr_model_ext* ext, double* u);
 
+/* Replaces save_solution(string, double* tspan, double* tspan_solns, int
+ * no_solns, user_data_struct) (src/save_solution.cpp:14; include/main.h:33):
+ * calibrates the micro-boundary entries of the no_solns + 1 rows of
+ * tspan_solns in place (as above), then writes the reference's file layout
+ * (the row count, then per row the time -- 0 for row 0 -- and the N values,
+ * printed as %.20e).  Returns TSR_ERR_IO where the reference prints an
+ * error and carries on. */
+int tsr_save_solution(const char* solution_file, const double* tspan, double* tspan_solns,
+                      int no_solns, const user_data_struct* user_data);
+
 /* Replaces phipade(double*, double*, double, int, int)
  * (src/phipade.cpp:15; include/exprem.h:28): phi_1(alpha*H(1:m,1:m)) by the
  * (6,6) Pade approximant with scaling and squaring, FP64 on the host.  H has
@@ -281,6 +291,16 @@ int tsr_profile_read(tsr_ctx* ctx, int category, double* ms, long long* count, d
 /* Replay each Arnoldi step of EXPREM from a captured CUDA graph (1, the
  * default) or launch its kernels one by one (0).  Same results either way. */
 int tsr_set_graphs(tsr_ctx* ctx, int enable);
+
+/* Dense-output rows of EXPREM calibrated on the device before they are
+ * copied out (1) -- the micro-boundary entries then hold the macro
+ * interpolant, as the reference's solution writer stores them -- or copied
+ * as computed (0, the default, the reference's exprem). */
+int tsr_set_calibrated_output(tsr_ctx* ctx, int enable);
+
+/* The same calibration of a device vector of this context's layout
+ * (asynchronous on the context stream). */
+int tsr_calibrate_device(tsr_ctx* ctx, double* d_x);
 
 /* Gram-Schmidt block of an Arnoldi step as one cooperative launch (1, the
  * default) or as the j + 4 separate reduction launches (0).  Same results

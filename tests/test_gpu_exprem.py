@@ -128,3 +128,40 @@ def test_fused_gram_schmidt_matches_separate_kernels():
     (ua, sa, sta, la), (ub, sb, stb, lb) = out
     assert la == lb and np.array_equal(ua, ub) and np.array_equal(sa, sb)
     assert sta.FuncEvals == stb.FuncEvals
+
+
+@pytest.mark.parametrize("make", [lambda: P.config1(), lambda: P.fixture10()], ids=["config1", "fixture10_quads"])
+def test_device_calibration_equals_host(make):
+    """tsr_calibrate_device (the solution writer's micro-boundary overwrite,
+    one warp per cell) gives the host calibration's bits."""
+    torch = pytest.importorskip("torch")
+    p = make()
+    lib = capi.load()
+    ctx = P.Context(p, max_krylov=0)
+    u = p.u0 + np.random.default_rng(4).normal(0.0, 0.5, p.N)
+    host = u.copy()
+    capi.check(lib.tsr_calibrate_micro_boundary(C.byref(p.ud), C.byref(p.ext), capi.ptr(host)), "host")
+    d = torch.from_numpy(u.copy()).to("cuda")
+    torch.cuda.synchronize()
+    capi.check(lib.tsr_calibrate_device(ctx.h, C.c_void_p(d.data_ptr())), "device")
+    capi.check(lib.tsr_sync(ctx.h), "sync")
+    assert np.array_equal(d.cpu().numpy(), host)
+    assert not np.array_equal(host, u)
+
+
+def test_calibrated_dense_output_rows():
+    """With calibrated output the saved rows are the oracle's rows after the
+    writer's calibration, bit for bit."""
+    p = P.config1()
+    p.tend = 0.05
+    p.tspan = np.array([2.0, 0.02, 0.05])
+    lib = capi.load()
+    ctx = P.Context(p)
+    capi.check(lib.tsr_set_calibrated_output(ctx.h, 1), "calibrated output")
+    ug, sg, stg, _ = P.run_to_end(ctx.exprem_step, p)
+    uo, so, sto, _ = P.run_to_end(oracle.Oracle(p, nthreads=8).exprem_step, p)
+    assert np.array_equal(ug, uo)
+    for k in (1, 2):
+        row = so[k].copy()
+        capi.check(lib.tsr_calibrate_micro_boundary(C.byref(p.ud), C.byref(p.ext), capi.ptr(row)), "host")
+        assert np.array_equal(sg[k], row)

@@ -93,6 +93,6 @@ def test_autotuned_packings_give_identical_bits():
     ctx = P.Context(p, max_krylov=0)
     g_default = ctx.g(p.u0)
     ms, thr, bud = ctx.autotune(p.u0, reps=2)
-    assert ms > 0 and thr in (128, 256, 512, 1024) and bud >= 48 * 1024
+    assert ms > 0 and thr % 32 == 0 and 128 <= thr <= 1024 and bud >= 48 * 1024
     assert np.array_equal(ctx.g(p.u0), g_default)
     assert np.array_equal(g_default, oracle.Oracle(p, nthreads=8).g(p.u0))

@@ -200,3 +200,67 @@ def test_reference_fixture_calibration_matches_reference_writer(tmp_path):
     untouched = np.setdiff1d(np.arange(p.N), idx)
     assert np.array_equal(u[untouched], MG.solution_state(p.N)[untouched])
     p.close()
+
+
+def test_solution_writer_matches_reference_layout(tmp_path):
+    """tsr_save_solution (the reference's save_solution: calibrate the
+    stored rows in place, then write them) on the reference's own scenario
+    read by this library: the same file layout as the reference's writer,
+    the same calibrated values as its golden output (1e-10, the interpolant
+    formulas differ in rounding), every other value exactly."""
+    from tests.helpers import FIXTURE, write_reference_fixture
+    from twoscalerich_gb300 import problem as P
+    g = np.load(FIXTURE)
+    p = P.from_reference_files(write_reference_fixture(str(tmp_path)))
+    u = MG.solution_state(p.N)
+    rows = np.concatenate([u, u + 1.0])          # two rows: t = 0 and t = tspan[1]
+    tspan = np.array([1.0, 0.25])
+    path = str(tmp_path / "solution.txt")
+    capi.check(capi.load().tsr_save_solution(path.encode(), capi.ptr(tspan), capi.ptr(rows), 1,
+                                             C.byref(p.ud)), "tsr_save_solution")
+    text = open(path).read()
+    lines = text.splitlines()
+    assert lines[0] == "2" and len(lines) == 3
+    tok0, tok1 = lines[1].split(" "), lines[2].split(" ")
+    assert tok0[0] == "0.00000000000000000000e+00" and tok1[0] == "%.20e" % 0.25
+    assert len(tok0) == p.N + 1
+    written = np.array(tok0[1:], dtype=float)
+    assert np.array_equal(written, rows[:p.N])       # in place, then written exactly
+    idx, ref = g["solution/index"], g["solution/value"]
+    assert np.max(np.abs(written[idx] - ref)) <= 1e-10 * np.max(np.abs(ref))
+    untouched = np.setdiff1d(np.arange(p.N), idx)
+    assert np.array_equal(written[untouched], u[untouched])
+    p.close()
+
+
+@pytest.mark.skipif(oracle.load_ref() is None, reason="oracle/_ref not present")
+def test_solution_writer_bytes_match_reference_writer(tmp_path):
+    """Byte for byte against the reference's own save_solution (compiled in
+    oracle/_ref) on rows whose micro-boundary entries are already calibrated
+    (so both writers see the same values)."""
+    ref = oracle.load_ref()
+    name, macro, micro, bc = MG.golden_meshes()[0]
+    M, m = _ours(macro, micro, bc)
+    ud = capi.UserData()
+    ud.macro_mesh, ud.micro_mesh, ud.model_type = M, m, 3
+    N = M.no_nodes + M.no_elements * m.no_nodes
+    ud.N = N
+    u = MG.solution_state(N)
+    capi.check(capi.load().tsr_calibrate_micro_boundary(C.byref(ud), None, capi.ptr(u)), "calibrate")
+    tspan = np.array([0.0])
+    ours, theirs = str(tmp_path / "ours.txt"), str(tmp_path / "ref.txt")
+    capi.check(capi.load().tsr_save_solution(ours.encode(), capi.ptr(tspan), capi.ptr(u.copy()), 0,
+                                             C.byref(ud)), "save")
+    # the reference's writer calibrates again with its own interpolant
+    # formula: the micro-boundary entries may differ in the last bits, every
+    # other token must be the same text
+    ref.ref_save_solution(theirs.encode(), capi.ptr(tspan), capi.ptr(u.copy()), 0, C.byref(ud))
+    a, b = open(ours).read().split(), open(theirs).read().split()
+    assert len(a) == len(b) == N + 2 and a[0] == b[0] == "1" and a[1] == b[1]
+    bnd = np.zeros(N, bool)
+    mb = capi.as_array(m.boundary_nodes, m.no_nodes, np.int32) == 1
+    for k in range(M.no_elements):
+        bnd[M.no_nodes + k * m.no_nodes:M.no_nodes + (k + 1) * m.no_nodes] = mb
+    assert all(a[2 + i] == b[2 + i] for i in np.nonzero(~bnd)[0])
+    va, vb = np.array(a[2:], dtype=float), np.array(b[2:], dtype=float)
+    assert np.max(np.abs(va - vb)) <= 1e-13 * np.max(np.abs(vb))

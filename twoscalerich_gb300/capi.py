@@ -149,6 +149,9 @@ _SIGNATURES = {
     "tsr_kernel_launches": (C.c_ulonglong, []),
     "tsr_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     "tsr_set_fused_gs": (C.c_int, [C.c_void_p, C.c_int]),
+    "tsr_set_calibrated_output": (C.c_int, [C.c_void_p, C.c_int]),
+    "tsr_calibrate_device": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "tsr_save_solution": (C.c_int, [C.c_char_p, dp, dp, C.c_int, C.POINTER(UserData)]),
     "tsr_wait_probe": (C.c_int, [C.c_int]),
     "tsr_fp64_peak": (C.c_int, [dp]),
     "tsr_mark": (C.c_int, [C.c_void_p, C.c_int]),

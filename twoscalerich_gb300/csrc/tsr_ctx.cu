@@ -109,6 +109,9 @@ struct tsr_ctx {
     // one captured graph per Arnoldi index j, with event nodes timing its
     // Jv and its Gram-Schmidt block
     bool use_graphs = true;
+    // dense-output rows calibrated on the device (the solution writer's
+    // micro-boundary overwrite) before they are copied out
+    bool calibrated_output = false;
     // the Gram-Schmidt block of an Arnoldi step as one cooperative launch
     bool fused_gs = true;
     int gs_grid = 0;
@@ -1568,7 +1571,11 @@ int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
             for (int k = 1; k <= ns; ++k) {
                 if (!(io.tspan[k] > z.t && io.tspan[k] <= tn)) continue;
                 double* row = rows + (size_t)k * (size_t)n;
-                if (z.m == 0) {
+                if (z.m == 0 && c->calibrated_output) {
+                    CK(cudaMemcpyAsync(c->d_x, c->d_u, sizeof(double) * (size_t)N, cudaMemcpyDeviceToDevice, s));
+                    launch_calibrate(c->P, c->d_x, s);
+                    CK(cudaMemcpyAsync(row, c->d_x + off, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, s));
+                } else if (z.m == 0) {
                     CK(cudaMemcpyAsync(row, c->d_u + off, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, s));
                 } else {
                     const double tau = io.tspan[k] - z.t;
@@ -1584,6 +1591,7 @@ int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
                                        cudaMemcpyHostToDevice, s));
                     if ((rc = set_active(c, mask_of({q})))) return rc;
                     launch_combine(c->d_u, V, N, c->d_coef, c->CS, c->d_mint, c->d_x, c->seg, s);
+                    if (c->calibrated_output) launch_calibrate(c->P, c->d_x, s);
                     CK(cudaMemcpyAsync(row, c->d_x + off, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, s));
                 }
                 CK(cudaStreamSynchronize(s));
@@ -1865,7 +1873,10 @@ extern "C" int tsr_autotune(tsr_ctx* c, const double* u_host, int reps, double* 
     CK(cudaMemcpyAsync(c->d_x, u_host, sizeof(double) * (size_t)c->N, cudaMemcpyHostToDevice, c->stream));
     int rc0 = all_active(c);
     if (rc0) return rc0;
-    const int thr[] = {128, 256, 512, 1024};
+    // block sizes include warp counts that divide the node and element
+    // counts of common templates evenly (the phases of a bundle wait for
+    // their slowest warp)
+    const int thr[] = {128, 160, 192, 224, 256, 288, 320, 384, 448, 512, 768, 1024};
     const int bud[] = {48 * 1024, 64 * 1024, 96 * 1024, 144 * 1024, 200 * 1024};
     double best = 1e30;
     int bt = c->tuned_threads, bb = c->tuned_budget;
@@ -1912,6 +1923,23 @@ extern "C" int tsr_set_graphs(tsr_ctx* c, int enable)
 {
     if (!c) return TSR_ERR_ARG;
     c->use_graphs = enable != 0;
+    return TSR_OK;
+}
+
+extern "C" int tsr_set_calibrated_output(tsr_ctx* c, int enable)
+{
+    if (!c) return TSR_ERR_ARG;
+    c->calibrated_output = enable != 0;
+    return TSR_OK;
+}
+
+extern "C" int tsr_calibrate_device(tsr_ctx* c, double* d_x)
+{
+    if (!c || !d_x) return TSR_ERR_ARG;
+    int rc = all_active(c);
+    if (rc) return rc;
+    launch_calibrate(c->P, d_x, c->stream);
+    CK(cudaGetLastError());
     return TSR_OK;
 }
 

@@ -248,6 +248,8 @@ void launch_relayout(const Problem& P, int Mn, int Ne, const long long* off_old,
 // water content terms, [macro nodes of s | cells of s] scenario by scenario
 // (reduce them with launch_vsum)
 void launch_water_terms(const Problem& P, const double* u, double* terms, cudaStream_t s);
+// micro-boundary entries of x <- the macro interpolant (solution writer calibration)
+void launch_calibrate(const Problem& P, double* x, cudaStream_t s);
 
 }  // namespace tsr
 

@@ -706,6 +706,43 @@ extern "C" int tsr_phipade(double* phiH, const double* H, double alpha, int m, i
 // before writing, their stored values are overwritten with the macro
 // interpolant at centroid_k + s vectors_l (model_type 1: the centroid).
 
+extern "C" int tsr_save_solution(const char* solution_file, const double* tspan, double* tspan_solns,
+                                 int no_solns, const user_data_struct* ud)
+{
+    if (!solution_file || !tspan || !tspan_solns || no_solns < 0) return TSR_ERR_ARG;
+    long long N = 0;
+    if (ud) {
+        N = (long long)ud->macro_mesh.no_nodes + (long long)ud->macro_mesh.no_elements * ud->micro_mesh.no_nodes;
+        // the reference calibrates the stored rows in place before writing
+        for (int j = 0; j <= no_solns; ++j) {
+            int rc = tsr_calibrate_micro_boundary(ud, nullptr, tspan_solns + (size_t)j * (size_t)N);
+            if (rc) return rc;
+        }
+    } else {
+        return TSR_ERR_ARG;
+    }
+    FILE* f = std::fopen(solution_file, "w");
+    if (!f) {
+        set_error(std::string("cannot open ") + solution_file);
+        return TSR_ERR_IO;
+    }
+    // the reference's layout: the row count, then per row the time and the
+    // N values, scientific with 20 digits after the point
+    bool ok = std::fprintf(f, "%d\n", no_solns + 1) > 0;
+    for (int j = 0; j <= no_solns && ok; ++j) {
+        ok = std::fprintf(f, "%.20e", j == 0 ? 0.0 : tspan[j]) > 0;
+        const double* row = tspan_solns + (size_t)j * (size_t)N;
+        for (long long k = 0; k < N && ok; ++k) ok = std::fprintf(f, " %.20e", row[k]) > 0;
+        ok = ok && std::fputc('\n', f) != EOF;
+    }
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) {
+        set_error(std::string("write failed: ") + solution_file);
+        return TSR_ERR_IO;
+    }
+    return TSR_OK;
+}
+
 extern "C" int tsr_calibrate_micro_boundary(const user_data_struct* ud, const tsr_model_ext* ext,
                                             double* u)
 {

@@ -1315,6 +1315,59 @@ __global__ void k_water_macro(Problem P, const double* __restrict__ u, double* _
 }
 
 // one warp per cell; lane l sums nodes l, l+32, ... (the fixed lane order)
+// The solution writer's calibration (src/save_solution.cpp:41-102): the
+// micro-boundary entries of state x, which the kernels never evolve (the
+// cells use the macro interpolant there), overwritten with the interpolant
+// at centroid + s vectors (model_type 1: the centroid); one warp per cell,
+// one lane per boundary node, the operation sequence of the host version
+// (tsr_calibrate_micro_boundary) and of the cell kernel's boundary pass.
+// Learned cells carry no micro nodes and are left alone.
+__global__ void k_calibrate(Problem P, double* __restrict__ x)
+{
+    const MacroDev& M = P.M;
+    const MicroSet& S = P.m;
+    const int lane = threadIdx.x & 31;
+    const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (k >= M.Ne) return;
+    const int nv = M.nv, Ne = M.Ne;
+    const TplDesc D = S.tpl[S.cell_tpl[k]];
+    if (D.kind != 0) return;
+    double al[4];
+    for (int m = 0; m < nv; ++m) {
+        long long v0 = M.elements[k];
+        if (M.node_off) v0 = M.node_off[v0];
+        double a = M.sf[(long long)(m * nv) * Ne + k] * x[v0];
+        for (int i = 1; i < nv; ++i) {
+            long long vi = M.elements[(long long)i * Ne + k];
+            if (M.node_off) vi = M.node_off[vi];
+            a = fma(M.sf[(long long)(m * nv + i) * Ne + k], x[vi], a);
+        }
+        al[m] = a;
+    }
+    const double s = P.cell_scale ? P.cell_scale[k] : 1.0;
+    const double cx = M.cent[k], cy = M.cent[Ne + k];
+    const int mn = D.mn;
+    const int* bl = S.bnl + D.bnl;
+    const double* vec = S.vec + 2 * D.node;
+    const long long off = S.cell_off[k];
+    for (int q = lane; q < D.nbn; q += 32) {
+        const int l = bl[q];
+        double px = cx, py = cy;
+        if (M.model_type != 1) {
+            px = fma(s, vec[l], cx);
+            py = fma(s, vec[mn + l], cy);
+        }
+        x[off + l] = interp_at(nv, al, px, py);
+    }
+}
+
+void launch_calibrate(const Problem& P, double* x, cudaStream_t s)
+{
+    count();
+    const long long threads = 32LL * P.M.Ne;
+    k_calibrate<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(P, x);
+}
+
 __global__ void k_water_cells(Problem P, const double* __restrict__ u, double* __restrict__ terms)
 {
     const MacroDev& M = P.M;
