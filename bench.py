@@ -455,6 +455,80 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_scale_to_end(args):
+    """Configs 2/3 from t = 0 towards t_end through device-resident EXPREM
+    steps, stopping at t_end or after --to-end-seconds of wall time, with
+    what limited every step (tsr_step_diagnostics).  The CPU wall time to the
+    same point is an ESTIMATE, labelled as such: the GPU run's G-evaluation
+    count divided by the G-evals/s the oracle's OpenMP EXPREM (C-library
+    log/exp) reaches on this machine stepping on from the GPU's final state (its
+    trajectory is the GPU's: the bitwise oracle takes the same steps)."""
+    from twoscalerich_gb300 import capi
+    from twoscalerich_gb300 import problem as P
+    if RANK != 0:
+        return
+    lib = capi.load()
+    p = make_problem(args)
+    ctx = P.Context(p, max_krylov=p.options.MaxKrylov)
+    h = ctx.h
+    ctx.autotune(p.u0, reps=2)
+    tspan = p.tspan.copy()
+    ns = int(tspan[0])
+    solns = np.zeros((ns + 1) * p.N)
+    solns[:p.N] = p.u0
+    capi.check(lib.tsr_set_calibrated_output(h, 1), "calibrated output")
+    capi.check(lib.tsr_exprem_load(h, capi.ptr(p.u0), 0.0), "load")
+    st = capi.ExpremStats()
+    t = C.c_double(0.0)
+    diag = np.zeros(8)
+    log = []
+    clocks = Clocks()
+    clocks.start()
+    capi.check(lib.tsr_sync(h), "sync")
+    w0 = time.perf_counter()
+    while t.value < p.tend and time.perf_counter() - w0 < args.to_end_seconds:
+        capi.check(lib.tsr_exprem_advance(h, p.tend, capi.ptr(tspan), capi.ptr(solns), C.byref(p.options),
+                                          C.byref(st), C.byref(t)), "tsr_exprem_advance")
+        capi.check(lib.tsr_step_diagnostics(h, 0, capi.ptr(diag)), "diagnostics")
+        log.append([t.value] + diag.tolist() + [st.FuncEvals])
+    capi.check(lib.tsr_sync(h), "sync")
+    wall = time.perf_counter() - w0
+    clk = clocks.stop()
+    L = np.array(log)
+    u_end = np.empty(p.N)
+    capi.check(lib.tsr_exprem_store(h, capi.ptr(u_end)), "store")
+    reached = t.value >= p.tend
+    if args.step_log:
+        with open(args.step_log, "w") as f:
+            f.write("# t dt_proposed dt_taken err krylov_halvings rejects growth_capped krylov_dim clipped func_evals\n")
+            for r in log:
+                f.write(" ".join("%.9g" % x for x in r) + "\n")
+    threads = os.cpu_count() or 1
+    cpu_rate, cpu_el, cpu_steps, cpu_evals = cpu_exprem_rate(p, u_end, t.value, st, threads, args.cpu_seconds)
+    last = L[-min(len(L), 200):]
+    line = {
+        "metric": "wall seconds to t_end (device-resident EXPREM steps, calibrated dense output)",
+        "value": wall if reached else None, "unit": "s", "n_gpus": 1, "higher_is_better": False,
+        "reached_t_end": bool(reached), "t_reached_days": t.value, "t_end_days": p.tend, "wall_s": wall,
+        "steps": int(st.NumSteps), "g_evals": int(st.FuncEvals), "dtype": "f64", "data": "synthetic",
+        "config": workload(args, p.N),
+        "steps_krylov_halved": int(np.sum(L[:, 4] > 0)), "steps_with_rejections": int(np.sum(L[:, 5] > 0)),
+        "steps_growth_capped": int(np.sum(L[:, 6] > 0)), "krylov_dim_mean": float(np.mean(L[:, 7])),
+        "krylov_dim_max": int(np.max(L[:, 7])),
+        "dt_taken_last200_p50": float(np.median(last[:, 2])),
+        "dt_taken_last200_p95": float(np.percentile(last[:, 2], 95)),
+        "cpu_estimate": {"wall_s_to_same_t": st.FuncEvals / cpu_rate, "unit": "s", "cores": threads,
+                         "kind": "port (ESTIMATE: GPU run's G evaluations / CPU G-evals/s)",
+                         "cpu_g_evals_per_s": cpu_rate,
+                         "sample": "%d accepted EXPREM steps (%d G evaluations) from the GPU's final state, "
+                                   "%.1f s" % (cpu_steps, cpu_evals, cpu_el)},
+        "clocks": clk,
+    }
+    line["speedup_vs_cpu_estimate"] = line["cpu_estimate"]["wall_s_to_same_t"] / wall
+    print(json.dumps(line))
+    ctx.close()
+
+
 def cpu_ensemble_rate(ens, seconds, threads=None):
     """Scenario-steps per second of the oracle's OpenMP EXPREM (C-library
     log/exp) on scenario 0 alone, stepped from t = 0 for about `seconds`."""
@@ -551,9 +625,16 @@ def run_ensemble(args):
         done_at = [None] * S
         w0 = time.perf_counter()
         rounds = 0
+        diag = np.zeros(8)
+        lim = np.zeros((S, 4))       # steps with Krylov halvings, rejections, growth cap; dim sum
         while True:
+            t_before = [st2[s].NumSteps for s in range(S)]
             t, status, nrun = ctx.ensemble_advance(st2)
             rounds += 1
+            for s in range(S):
+                if st2[s].NumSteps > t_before[s]:
+                    capi.check(lib.tsr_step_diagnostics(h, s, capi.ptr(diag)), "diagnostics")
+                    lim[s] += [diag[3] > 0, diag[4] > 0, diag[5] > 0, diag[6]]
             now = time.perf_counter() - w0
             for s in range(S):
                 if done_at[s] is None and (t[s] >= p.tend or status[s] != 0):
@@ -568,7 +649,11 @@ def run_ensemble(args):
                   "t_reached_p5_p50_p95": [float(np.percentile(t, q)) for q in (5, 50, 95)],
                   "steps_per_scenario": [st2[s].NumSteps for s in range(S)],
                   "failed": int(sum(1 for s in range(S) if status[s] != 0)),
-                  "scenario_steps_per_s": sum(st2[s].NumSteps for s in range(S)) / now}
+                  "scenario_steps_per_s": sum(st2[s].NumSteps for s in range(S)) / now,
+                  "limiters": {"steps": int(sum(st2[s].NumSteps for s in range(S))),
+                               "krylov_halved": int(lim[:, 0].sum()), "with_rejections": int(lim[:, 1].sum()),
+                               "growth_capped": int(lim[:, 2].sum()),
+                               "krylov_dim_mean": float(lim[:, 3].sum() / max(1, sum(st2[s].NumSteps for s in range(S))))}}
     cpu = None
     if RANK == 0 and WORLD == 1 and not args.no_cpu_baseline:
         cpu = cpu_ensemble_rate(p, args.cpu_seconds)
@@ -754,9 +839,12 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
                     help="minimum seconds of CPU work in the CPU baseline sample")
     ap.add_argument("--to-end", action="store_true",
-                    help="config 4: also run every scenario to t_end (p50/p95 wall time)")
+                    help="config 4: also run every scenario to t_end (p50/p95 wall time); "
+                         "configs 2-3: run to t_end instead of the timed steps")
     ap.add_argument("--to-end-seconds", type=float, default=600.0,
-                    help="config 4: wall-time cap of the run to t_end")
+                    help="configs 2-4: wall-time cap of the run to t_end")
+    ap.add_argument("--step-log", default=None,
+                    help="configs 2-3 with --to-end: write the per-step limiter record to this file")
     args = ap.parse_args()
     if args.config == 3 and args.n_macro == 201:
         args.n_macro = 151
@@ -777,6 +865,8 @@ def main():
         run_closure_bench(args)
     elif args.config == 1:
         run_to_end_bench(args)
+    elif args.to_end:
+        run_scale_to_end(args)
     else:
         run_ours(args)
 

@@ -96,6 +96,24 @@ int tsr_calibrate_micro_boundary(const user_data_struct* user_data,
 int tsr_save_solution(const char* solution_file, const double* tspan, double* tspan_solns,
                       int no_solns, const user_data_struct* user_data);
 
+/* Keff(h) by homogenisation of the unit cell -- the table the reference
+ * reads (src/read_effective_conductivity.cpp; include/Keff.h) and generates
+ * with a MATLAB script it does not ship (src/main.cpp:111-112).  The macro
+ * continuum is material A around the inclusion, whose triangles are
+ * `inclusion` (a micro mesh, cell_width x cell_height cell, inclusion not
+ * touching the cell boundary).  Solves the periodic cell problems of the
+ * perforated cell (cut-face finite volumes on a resolution-wide grid,
+ * conjugate gradients on the GPU to relative residual tol) and returns
+ * Khom[4] (row-major: e_c . <grad chi_d + e_d>, K_A = 1) and epsA = |Y_A| /
+ * |Y|.  With n_h > 0 it also fills table[5 * n_h] in the reference's
+ * component-major layout: log10|h| = logh_first + r logr, then
+ * K11, K12, K21, K22 = factor * K_A(10^log10|h|) * Khom (K_A the van
+ * Genuchten-Mualem conductivity of soilA; factor converts its time unit). */
+int tsr_keff_homogenize(const micro_mesh_struct* inclusion, double cell_width, double cell_height,
+                        int resolution, double tol, const soil_struct* soilA, double factor,
+                        double logh_first, double logr, int n_h, double* Khom, double* epsA,
+                        double* table);
+
 /* Replaces phipade(double*, double*, double, int, int)
  * (src/phipade.cpp:15; include/exprem.h:28): phi_1(alpha*H(1:m,1:m)) by the
  * (6,6) Pade approximant with scaling and squaring, FP64 on the host.  H has
@@ -291,6 +309,14 @@ int tsr_profile_read(tsr_ctx* ctx, int category, double* ms, long long* count, d
 /* Replay each Arnoldi step of EXPREM from a captured CUDA graph (1, the
  * default) or launch its kernels one by one (0).  Same results either way. */
 int tsr_set_graphs(tsr_ctx* ctx, int enable);
+
+/* What shaped scenario s's last accepted step (no counterpart in the
+ * reference; 8 doubles): the step size proposed at its start, the size
+ * taken, the accepted error estimate (weighted RMS, accept at <= 1), the
+ * halvings because the Krylov space at the largest dimension was too small,
+ * the rejected attempts, 1 if the next proposal was capped by
+ * MaxStepIncFac, the Krylov dimension, 1 if the step was clipped to tend. */
+int tsr_step_diagnostics(tsr_ctx* ctx, int s, double* out);
 
 /* Dense-output rows of EXPREM calibrated on the device before they are
  * copied out (1) -- the micro-boundary entries then hold the macro

@@ -150,6 +150,10 @@ _SIGNATURES = {
     "tsr_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     "tsr_set_fused_gs": (C.c_int, [C.c_void_p, C.c_int]),
     "tsr_set_calibrated_output": (C.c_int, [C.c_void_p, C.c_int]),
+    "tsr_step_diagnostics": (C.c_int, [C.c_void_p, C.c_int, dp]),
+    "tsr_keff_homogenize": (C.c_int, [C.POINTER(MicroMesh), C.c_double, C.c_double, C.c_int, C.c_double,
+                                      C.POINTER(Soil), C.c_double, C.c_double, C.c_double, C.c_int,
+                                      dp, dp, dp]),
     "tsr_calibrate_device": (C.c_int, [C.c_void_p, C.c_void_p]),
     "tsr_save_solution": (C.c_int, [C.c_char_p, dp, dp, C.c_int, C.POINTER(UserData)]),
     "tsr_wait_probe": (C.c_int, [C.c_int]),

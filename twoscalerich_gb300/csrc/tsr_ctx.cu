@@ -48,6 +48,12 @@ struct ScenState {
     int m = 0, maxk = 0;
     int m_prev = 0;              // Krylov dimension of the last accepted step
     std::vector<double> Hm, phi, cv, z;
+    // what limited the last accepted step: its proposed size, the number of
+    // halvings because the Krylov space was too small at the largest
+    // dimension, the rejected attempts, the error of the accepted attempt,
+    // and whether the next step's growth was capped by MaxStepIncFac
+    double diag_dt0 = 0.0, diag_err = 0.0;
+    int diag_krylov_cuts = 0, diag_rejects = 0, diag_capped = 0, diag_clipped = 0;
 };
 
 }  // namespace
@@ -1276,9 +1282,14 @@ int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
         z.dt = st.CurrentStep;
         if (z.dt > opt->MaxStep) z.dt = opt->MaxStep;
         z.last = false;
+        z.diag_dt0 = z.dt;
+        z.diag_krylov_cuts = 0;
+        z.diag_rejects = 0;
+        z.diag_clipped = 0;
         if (z.t + z.dt >= io.tend) {
             z.dt = io.tend - z.t;
             z.last = true;
+            z.diag_clipped = 1;
         }
         live.push_back(q);
     }
@@ -1472,6 +1483,7 @@ int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
         while (z.errK > kKrylovTol) {
             const double f = 0.5 > opt->MinStepDecFac ? 0.5 : opt->MinStepDecFac;
             z.dt = z.dt * f;
+            z.diag_krylov_cuts++;
             z.last = false;
             if (z.dt < opt->MinStep) {
                 fail(q, TSR_ERR_MINSTEP, "step size below MinStep (Krylov)");
@@ -1553,6 +1565,7 @@ int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
             if (fac > 1.0) fac = opt->MinStepDecFac;
             z.dt = z.dt * fac;
             z.last = false;
+            z.diag_rejects++;
             if (z.dt < opt->MinStep) {
                 fail(q, TSR_ERR_MINSTEP, "step size below MinStep");
                 continue;
@@ -1611,6 +1624,8 @@ int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
             const double tn = z.last ? io.tend : z.t + z.dt;
             z.t = tn;
             double fac = (z.err > 0.0) ? opt->SafetyFac * std::pow(z.err, -1.0 / 3.0) : opt->MaxStepIncFac;
+            z.diag_capped = fac >= opt->MaxStepIncFac;
+            z.diag_err = z.err;
             if (fac > opt->MaxStepIncFac) fac = opt->MaxStepIncFac;
             if (fac < opt->MinStepDecFac) fac = opt->MinStepDecFac;
             double dn = z.dt * fac;
@@ -1923,6 +1938,21 @@ extern "C" int tsr_set_graphs(tsr_ctx* c, int enable)
 {
     if (!c) return TSR_ERR_ARG;
     c->use_graphs = enable != 0;
+    return TSR_OK;
+}
+
+extern "C" int tsr_step_diagnostics(tsr_ctx* c, int s, double* out)
+{
+    if (!c || !out || s < 0 || s >= c->S) return TSR_ERR_ARG;
+    const ScenState& z = c->sc[s];
+    out[0] = z.diag_dt0;
+    out[1] = z.dt;
+    out[2] = z.diag_err;
+    out[3] = z.diag_krylov_cuts;
+    out[4] = z.diag_rejects;
+    out[5] = z.diag_capped;
+    out[6] = z.m;
+    out[7] = z.diag_clipped;
     return TSR_OK;
 }
 
