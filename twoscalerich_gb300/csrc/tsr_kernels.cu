@@ -1102,8 +1102,12 @@ __global__ void __launch_bounds__(kRedThreads, 1) k_gs_cluster(SegInfo g, GsArgs
         }
         cl.sync();
     }
-    // the weighted norm of v_{j+1} (total of the last pass), and w
-    if (writer && act) A.sv[so] = seg_total((j + 2) & 1);
+    // the weighted norm of v_{j+1} (total of the last pass): every lane of
+    // warp 0 takes part in the warp shuffles, lane 0 stores; then w
+    if (b == B.b0 && act && (threadIdx.x >> 5) == 0) {
+        const double sv = seg_total((j + 2) & 1);
+        if (threadIdx.x == 0) A.sv[so] = sv;
+    }
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
         const long long i = base + (long long)q * kRedThreads;
