@@ -202,6 +202,15 @@ def workload(args, N):
             "parallelism": "replicas" if WORLD > 1 else "1 GPU"}
 
 
+def cell_plan(lib, h):
+    """The cell kernel's plan after autotuning."""
+    from twoscalerich_gb300 import capi
+    out = (C.c_int * 6)()
+    capi.check(lib.tsr_cell_plan(h, out), "tsr_cell_plan")
+    return {"tables_in_shared_memory": bool(out[2]), "cells_per_bundle_max": out[3], "grid": out[4],
+            "smem_per_cta": out[5]}
+
+
 def repo_libraries():
     """Shared libraries of this repository mapped into the process (Linux)."""
     found = set()
@@ -444,8 +453,8 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * N,
                 "d2h_bytes_per_step": 8 * N},
         "gpu_launches": int(launches),
-        "autotuned": None if tuned is None else {"g_ms": tuned[0], "threads": tuned[1],
-                                                 "smem_budget": tuned[2]},
+        "autotuned": None if tuned is None else dict({"g_ms": tuned[0], "threads": tuned[1],
+                                                      "smem_budget": tuned[2]}, **cell_plan(lib, h)),
         "cpu_baseline": cpu,
     }
     if RANK == 0:

@@ -306,6 +306,16 @@ int tsr_cell_summary(tsr_ctx* ctx, const double* u, double* out);
 int tsr_profile(tsr_ctx* ctx, int enable);
 int tsr_profile_read(tsr_ctx* ctx, int category, double* ms, long long* count, double* bytes);
 
+/* The cell kernel's current plan (6 ints): threads per CTA, shared-memory
+ * budget, 1 if the math tables sit in shared memory (0: read through L1),
+ * most cells per bundle, persistent grid, dynamic shared memory per CTA. */
+int tsr_cell_plan(tsr_ctx* ctx, int* out);
+
+/* A plan of the caller's choosing (what the autotuner sets): threads per
+ * CTA (64-1024, a multiple of 32), shared-memory budget in bytes, tables in
+ * shared memory (1) or read through L1 (0).  Results never depend on it. */
+int tsr_set_cell_plan(tsr_ctx* ctx, int threads, int budget, int tables_smem);
+
 /* Replay each Arnoldi step of EXPREM from a captured CUDA graph (1, the
  * default) or launch its kernels one by one (0).  Same results either way. */
 int tsr_set_graphs(tsr_ctx* ctx, int enable);

@@ -96,3 +96,24 @@ def test_autotuned_packings_give_identical_bits():
     assert ms > 0 and thr % 32 == 0 and 128 <= thr <= 1024 and bud >= 48 * 1024
     assert np.array_equal(ctx.g(p.u0), g_default)
     assert np.array_equal(g_default, oracle.Oracle(p, nthreads=8).g(p.u0))
+
+
+@pytest.mark.parametrize("make", [lambda: P.config3(n_macro=21), lambda: P.config2(n_macro=21, n_micro=21)],
+                         ids=["config3_batched", "config2_21x21_cells"])
+def test_cell_plans_give_identical_bits(make):
+    """Block sizes, shared-memory budgets (cells per bundle) and the place
+    of the math tables (shared memory or read through L1) change the speed
+    of the cell kernel, never its bits."""
+    import ctypes as C
+    from twoscalerich_gb300 import capi
+    p = make()
+    lib = capi.load()
+    ctx = P.Context(p, max_krylov=0)
+    ref = oracle.Oracle(p, nthreads=8).g(p.u0)
+    plan = (C.c_int * 6)()
+    for threads, budget, tables in ((224, 64 * 1024, 1), (224, 64 * 1024, 0), (448, 144 * 1024, 0),
+                                    (160, 48 * 1024, 1), (1024, 200 * 1024, 0)):
+        capi.check(lib.tsr_set_cell_plan(ctx.h, threads, budget, tables), "plan")
+        capi.check(lib.tsr_cell_plan(ctx.h, plan), "read plan")
+        assert plan[0] == threads and plan[2] == tables
+        assert np.array_equal(ctx.g(p.u0), ref)

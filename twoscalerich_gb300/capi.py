@@ -151,6 +151,8 @@ _SIGNATURES = {
     "tsr_set_fused_gs": (C.c_int, [C.c_void_p, C.c_int]),
     "tsr_set_calibrated_output": (C.c_int, [C.c_void_p, C.c_int]),
     "tsr_step_diagnostics": (C.c_int, [C.c_void_p, C.c_int, dp]),
+    "tsr_cell_plan": (C.c_int, [C.c_void_p, ip]),
+    "tsr_set_cell_plan": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "tsr_keff_homogenize": (C.c_int, [C.POINTER(MicroMesh), C.c_double, C.c_double, C.c_int, C.c_double,
                                       C.POINTER(Soil), C.c_double, C.c_double, C.c_double, C.c_int,
                                       dp, dp, dp]),

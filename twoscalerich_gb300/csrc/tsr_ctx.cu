@@ -109,7 +109,7 @@ struct tsr_ctx {
     std::vector<int> cell_tpl_host;
     int* d_bundle = nullptr;     // 3 * Ne ints (tpl, first, count) + Ne cell ids
     int nsm = 0, dev_smem = 0;
-    int tuned_threads = 0, tuned_budget = 0;
+    int tuned_threads = 0, tuned_budget = 0, tuned_tables = 1;
     // finite-difference step {eps, 1/eps}, staged through pinned memory
     double* h_eps = nullptr;
     // one captured graph per Arnoldi index j, with event nodes timing its
@@ -224,11 +224,11 @@ Csr group_events(int n_nodes, const std::vector<int>& node, const std::vector<in
 
 constexpr int kMiscSlots = 32;     // most cells in one bundle
 
-// shared memory of a bundle plan: tables, per-cell scratch, the largest
-// bundle's state
-size_t cell_smem(int slots, size_t state_doubles)
+// shared memory of a bundle plan: tables (when copied there), per-cell
+// scratch, the largest bundle's state
+size_t cell_smem(int slots, size_t state_doubles, bool tables)
 {
-    return sizeof(tsr_math_tables) + sizeof(double) * 16 * (size_t)slots +
+    return (tables ? sizeof(tsr_math_tables) : 0) + sizeof(double) * 16 * (size_t)slots +
            (sizeof(long long) + 2 * sizeof(int)) * (size_t)slots + sizeof(double) * state_doubles;
 }
 
@@ -239,7 +239,7 @@ namespace tsr {
 // Packs cells into bundles (cells of one template, as many as fit in the
 // shared-memory budget, at most kMiscSlots), largest templates first, and
 // sets the persistent grid of the cell kernel for `threads` per CTA.
-int plan_cells(tsr_ctx* c, int threads, int budget)
+int plan_cells(tsr_ctx* c, int threads, int budget, int tables_smem)
 {
     Problem& P = c->P;
     // captured graphs hold the old launch shape
@@ -249,7 +249,7 @@ int plan_cells(tsr_ctx* c, int threads, int budget)
             g = nullptr;
         }
     const int ntpl = (int)c->tpl_host.size();
-    const size_t fixed = cell_smem(kMiscSlots, 0);
+    const size_t fixed = cell_smem(kMiscSlots, 0, tables_smem != 0);
     std::vector<int> per(ntpl, 1);
     size_t max_state = 0;
     for (int t = 0; t < ntpl; ++t) {
@@ -260,7 +260,9 @@ int plan_cells(tsr_ctx* c, int threads, int budget)
         per[t] = (int)fit;
         if ((size_t)per[t] * st > max_state) max_state = (size_t)per[t] * st;
     }
-    const size_t smem = cell_smem(kMiscSlots, max_state);
+    // scratch slots for the largest bundle only
+    const int slots = *std::max_element(per.begin(), per.end());
+    const size_t smem = cell_smem(slots, max_state, tables_smem != 0);
     if (smem > (size_t)c->dev_smem) {
         set_error("a micro cell does not fit in shared memory");
         return TSR_ERR_ARG;
@@ -297,10 +299,11 @@ int plan_cells(tsr_ctx* c, int threads, int budget)
     S.bundle_first = c->d_bundle + nbun;
     S.bundle_count = c->d_bundle + 2 * nbun;
     S.bundle_cells = c->d_bundle + 3 * nbun;
-    S.maxc = *std::max_element(per.begin(), per.end());
-    P.misc_slots = kMiscSlots;
+    S.maxc = slots;
+    P.misc_slots = slots;
     P.micro_block = threads;
     P.micro_smem = smem;
+    P.tables_smem = tables_smem;
     int occ = 1;
     int rc = configure_cell_kernels(P, &occ);
     if (rc) return rc;
@@ -309,6 +312,7 @@ int plan_cells(tsr_ctx* c, int threads, int budget)
     if (P.micro_grid < 1) P.micro_grid = 1;
     c->tuned_threads = threads;
     c->tuned_budget = budget;
+    c->tuned_tables = tables_smem;
     return TSR_OK;
 }
 
@@ -705,7 +709,7 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
         int v = std::atoi(e);
         if (v >= 64 && v <= 1024 && v % 32 == 0) threads = v;
     }
-    return tsr::plan_cells(c, threads, 48 * 1024);
+    return tsr::plan_cells(c, threads, 48 * 1024, 1);
 }
 
 // Segments of `start` (S+1 offsets) for the reduction kernels.
@@ -1907,10 +1911,12 @@ extern "C" int tsr_autotune(tsr_ctx* c, const double* u_host, int reps, double* 
     } guard{&e0, &e1};
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
+    int bs = c->tuned_tables;
+    for (int tab : {1, 0})
     for (int T : thr)
         for (int B : bud) {
             if (B > c->dev_smem) continue;
-            if (tsr::plan_cells(c, T, B) != TSR_OK) continue;
+            if (tsr::plan_cells(c, T, B, tab) != TSR_OK) continue;
             launch_g(c->P, 0, c->d_x, nullptr, nullptr, nullptr, c->d_y, c->stream);   // warm
             CK(cudaEventRecord(e0, c->stream));
             for (int r = 0; r < reps; ++r)
@@ -1924,13 +1930,33 @@ extern "C" int tsr_autotune(tsr_ctx* c, const double* u_host, int reps, double* 
                 best = ms / reps;
                 bt = T;
                 bb = B;
+                bs = tab;
             }
         }
-    int rc = tsr::plan_cells(c, bt, bb);
+    int rc = tsr::plan_cells(c, bt, bb, bs);
     if (rc) return rc;
     if (best_ms) *best_ms = best;
     if (best_threads) *best_threads = bt;
     if (best_budget) *best_budget = bb;
+    return TSR_OK;
+}
+
+extern "C" int tsr_set_cell_plan(tsr_ctx* c, int threads, int budget, int tables_smem)
+{
+    if (!c || threads < 64 || threads > 1024 || threads % 32 != 0 || budget < 0 || budget > c->dev_smem)
+        return TSR_ERR_ARG;
+    return tsr::plan_cells(c, threads, budget, tables_smem ? 1 : 0);
+}
+
+extern "C" int tsr_cell_plan(tsr_ctx* c, int* out)
+{
+    if (!c || !out) return TSR_ERR_ARG;
+    out[0] = c->P.micro_block;
+    out[1] = c->tuned_budget;
+    out[2] = c->P.tables_smem;
+    out[3] = c->P.m.maxc;
+    out[4] = c->P.micro_grid;
+    out[5] = (int)c->P.micro_smem;
     return TSR_OK;
 }
 
@@ -2041,7 +2067,7 @@ int relayout(tsr_ctx* c, const std::vector<int>& learned_new)
     int rc;
     if ((rc = make_seg(c, c->scen_start, &c->seg))) return rc;
     c->sc[0].g0_valid = false;
-    return tsr::plan_cells(c, c->tuned_threads, c->tuned_budget);
+    return tsr::plan_cells(c, c->tuned_threads, c->tuned_budget, c->tuned_tables);
 }
 
 ClosureDev closure_dev(tsr_ctx* c)

@@ -100,6 +100,7 @@ struct Problem {
     int kface;
     int micro_block;            // threads per cell CTA
     size_t micro_smem;          // dynamic shared memory per cell CTA
+    int tables_smem;            // 1: the math tables copied into shared memory; 0: read through L1
     int micro_grid;             // persistent grid of the cell kernel
     int misc_slots;             // per-cell scratch slots reserved in shared memory
     double* contrib;            // [16*Ne] macro contributions per element

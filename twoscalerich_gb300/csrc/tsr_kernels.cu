@@ -267,7 +267,7 @@ __device__ __forceinline__ void macro_element_terms(const Problem& P, int k, con
 // and the threads sweep the bundle's flattened node and element index
 // spaces.  Every cell still follows the single-cell operation sequence (the
 // same as the host oracle), so packing changes speed, never bits.
-template <int MODE>
+template <int MODE, bool STAB>
 __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restrict__ u,
                                                 const double* __restrict__ v,
                                                 const double* __restrict__ g0,
@@ -277,9 +277,12 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
     // The finite-difference step and its reciprocal come from device memory
     // (one pair per scenario) so that a captured graph replays with the
     // current values; cells of scenarios that are not active are skipped.
+    // STAB: the math tables are copied into shared memory once per CTA;
+    // otherwise they are read from global memory through L1 (14 KB less
+    // shared memory per CTA, more CTAs per SM)
     extern __shared__ double sm[];
-    tsr_math_tables* T = reinterpret_cast<tsr_math_tables*>(sm);
-    double* misc = sm + kTabDoubles;                         // 16 per cell slot
+    const tsr_math_tables* T = STAB ? reinterpret_cast<const tsr_math_tables*>(sm) : &d_tables;
+    double* misc = sm + (STAB ? kTabDoubles : 0);            // 16 per cell slot
     long long* coff = reinterpret_cast<long long*>(misc + 16 * P.misc_slots);
     int* ck = reinterpret_cast<int*>(coff + P.misc_slots);
     double* st = reinterpret_cast<double*>(ck + 2 * P.misc_slots);
@@ -289,7 +292,7 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
     const MicroSet& S = P.m;
     const int nv = M.nv, Ne = M.Ne;
     const bool exch = (M.model_type == 3);
-    load_tables(T);
+    if (STAB) load_tables(reinterpret_cast<tsr_math_tables*>(sm));
     int* cscen = ck + P.misc_slots;                          // scenario of each cell, -1 inactive
     for (int b = blockIdx.x; b < S.n_bundles; b += gridDim.x) {
         const int t = S.bundle_tpl[b], first = S.bundle_first[b], nc = S.bundle_count[b];
@@ -551,13 +554,13 @@ __global__ void __launch_bounds__(128) k_macro_nodes(Problem P, const double* __
 
 int configure_cell_kernels(const Problem& P, int* occ)
 {
-    cudaError_t e = cudaFuncSetAttribute(k_cells<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)P.micro_smem);
+    cudaError_t e = cudaSuccess;
+    for (auto f : {k_cells<0, true>, k_cells<1, true>, k_cells<0, false>, k_cells<1, false>})
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.micro_smem);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_cells<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)P.micro_smem);
-    if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, k_cells<0>, P.micro_block, P.micro_smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            occ, P.tables_smem ? k_cells<0, true> : k_cells<0, false>, P.micro_block, P.micro_smem);
     if (e != cudaSuccess) {
         set_error(std::string("configuring the cell kernel: ") + cudaGetErrorString(e));
         return 1;
@@ -572,10 +575,16 @@ void launch_g(const Problem& P, int mode, const double* u, const double* v, cons
     const int nb = (P.M.Mn + 127) / 128;
     count(2);
     if (mode == 0) {
-        k_cells<0><<<P.micro_grid, P.micro_block, P.micro_smem, s>>>(P, u, v, g0, epsv, out);
+        if (P.tables_smem)
+            k_cells<0, true><<<P.micro_grid, P.micro_block, P.micro_smem, s>>>(P, u, v, g0, epsv, out);
+        else
+            k_cells<0, false><<<P.micro_grid, P.micro_block, P.micro_smem, s>>>(P, u, v, g0, epsv, out);
         k_macro_nodes<0><<<nb, 128, 0, s>>>(P, u, v, g0, epsv, out);
     } else {
-        k_cells<1><<<P.micro_grid, P.micro_block, P.micro_smem, s>>>(P, u, v, g0, epsv, out);
+        if (P.tables_smem)
+            k_cells<1, true><<<P.micro_grid, P.micro_block, P.micro_smem, s>>>(P, u, v, g0, epsv, out);
+        else
+            k_cells<1, false><<<P.micro_grid, P.micro_block, P.micro_smem, s>>>(P, u, v, g0, epsv, out);
         k_macro_nodes<1><<<nb, 128, 0, s>>>(P, u, v, g0, epsv, out);
     }
 }
