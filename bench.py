@@ -40,6 +40,7 @@ sys.path.insert(0, ROOT)
 
 WORLD = int(os.environ.get("WORLD_SIZE", "1"))
 RANK = int(os.environ.get("RANK", "0"))
+GS = {"mgs": 0, "cgs2": 1}          # Arnoldi orthogonalisation variants (tsr_set_gram_schmidt)
 LOCAL_RANK = int(os.environ.get("LOCAL_RANK", "0"))
 if WORLD > 1:
     # one GPU per rank: the library's CUDA runtime sees only this rank's GPU
@@ -175,6 +176,12 @@ def l2_statement(args, N):
 
 
 def workload(args, N):
+    w = _workload(args, N)
+    w["orthogonalisation"] = {"mgs": "modified Gram-Schmidt", "cgs2": "classical Gram-Schmidt twice"}[args.gs]
+    return w
+
+
+def _workload(args, N):
     if args.config == 4:
         return {"workload": "two-scale Richards ensemble, independent EXPREM per scenario",
                 "scenarios": args.scenarios,
@@ -323,7 +330,7 @@ def run_ours(args):
     lib = capi.load()
     p = make_problem(args)
     N = p.N
-    ctx = P.Context(p, max_krylov=p.options.MaxKrylov)
+    ctx = P.Context(p, max_krylov=p.options.MaxKrylov, gram_schmidt=GS[args.gs])
     h = ctx.h
     tuned = ctx.autotune(p.u0, reps=2)     # packing and block size of the cell kernel
     fp64_peak = C.c_double()
@@ -478,7 +485,7 @@ def run_scale_to_end(args):
         return
     lib = capi.load()
     p = make_problem(args)
-    ctx = P.Context(p, max_krylov=p.options.MaxKrylov)
+    ctx = P.Context(p, max_krylov=p.options.MaxKrylov, gram_schmidt=GS[args.gs])
     h = ctx.h
     ctx.autotune(p.u0, reps=2)
     tspan = p.tspan.copy()
@@ -573,7 +580,7 @@ def run_ensemble(args):
     lib = capi.load()
     p = make_problem(args)
     N, S = p.N, p.S
-    ctx = P.Context(p, max_krylov=p.options.MaxKrylov)
+    ctx = P.Context(p, max_krylov=p.options.MaxKrylov, gram_schmidt=GS[args.gs])
     h = ctx.h
     tuned = ctx.autotune(p.u0, reps=2)
     stats = (capi.ExpremStats * S)()
@@ -706,7 +713,7 @@ def run_to_end_bench(args):
     if RANK != 0:
         return
     p = P.config1()
-    ctx = P.Context(p)
+    ctx = P.Context(p, gram_schmidt=GS[args.gs])
     for _ in range(args.warmup):                      # warm: one full run
         P.run_to_end(ctx.exprem_step, p)
     clocks = Clocks()
@@ -732,6 +739,7 @@ def run_to_end_bench(args):
         "ms_per_step": 1e3 * gpu_s / max(st.NumSteps, 1), "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "two-scale Richards, 21x21 macro, 11x11 micro, t_end = 1 d",
+                   "orthogonalisation": {"mgs": "modified Gram-Schmidt", "cgs2": "classical Gram-Schmidt twice"}[args.gs],
                    "unknowns": p.N, "accepted_steps": st.NumSteps, "g_evals": st.FuncEvals,
                    "inputs_vs_l2": "working set 0.4 GB of vectors and basis; repeated runs"},
         "runs_s": runs,
@@ -847,6 +855,8 @@ def main():
     ap.add_argument("--scenarios", type=int, default=64)
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
                     help="minimum seconds of CPU work in the CPU baseline sample")
+    ap.add_argument("--gs", default="mgs", choices=sorted(GS),
+                    help="Arnoldi orthogonalisation: modified Gram-Schmidt (the reference's) or classical twice")
     ap.add_argument("--to-end", action="store_true",
                     help="config 4: also run every scenario to t_end (p50/p95 wall time); "
                          "configs 2-3: run to t_end instead of the timed steps")

@@ -343,6 +343,18 @@ int tsr_calibrate_device(tsr_ctx* ctx, double* d_x);
  * either way. */
 int tsr_set_fused_gs(tsr_ctx* ctx, int enable);
 
+/* Orthogonalisation of the Arnoldi step (the modified Gram-Schmidt loop
+ * inside the reference's missing exprem, called at src/main.cpp:316-322):
+ * 0 modified Gram-Schmidt, the default, in the reference's order; 1
+ * classical Gram-Schmidt twice (CGS2): H(i, j) = c_i + d_i from two
+ * classical passes, each dot a fixed-order reduction, four barriers and
+ * 3j+10 vector passes of traffic per Arnoldi step instead of j+3 and 4j+8.
+ * Its trajectories differ from modified Gram-Schmidt's by rounding and the
+ * step decisions that rounding moves; they are bitwise those of the oracle
+ * run with the same variant.  CGS2 takes Krylov dimensions up to 63
+ * (TSR_ERR_ARG beyond). */
+int tsr_set_gram_schmidt(tsr_ctx* ctx, int variant);
+
 /* Failure paths of the bounded device waits, run on purpose (tests):
  * which = 0, the grid barrier of the fused Gram-Schmidt kernel with a CTA
  * that never arrives; 1, the tensor-core MMA barrier with nothing arriving.

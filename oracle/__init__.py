@@ -53,6 +53,7 @@ def load(libm=False):
         _sig(lib, "oracle_exprem_step", C.c_int, [vp, dp, C.c_double, dp, dp, dp,
                                                   C.POINTER(capi.ExpremOptions),
                                                   C.POINTER(capi.ExpremStats), C.c_int])
+        _sig(lib, "oracle_set_gram_schmidt", C.c_int, [vp, C.c_int])
         for f in ("log", "exp", "expm1", "log1p"):
             _sig(lib, "oracle_math_" + f, C.c_double, [C.c_double])
         _sig(lib, "oracle_math_log1p_unit", C.c_double, [C.c_double, dp])
@@ -116,12 +117,15 @@ def load_ref():
 class Oracle:
     """The oracle bound to one problem (twoscalerich_gb300.problem.Problem)."""
 
-    def __init__(self, problem, nthreads=1, libm=False):
+    def __init__(self, problem, nthreads=1, libm=False, gram_schmidt=0):
+        """gram_schmidt: 0 modified Gram-Schmidt, 1 classical twice (CGS2)."""
         self.lib = load(libm)
         self.p = problem
         self.h = self.lib.oracle_create(C.byref(problem.ud), C.byref(problem.ext))
         if not self.h:
             raise RuntimeError("oracle_create failed")
+        if self.lib.oracle_set_gram_schmidt(self.h, gram_schmidt) != 0:
+            raise ValueError("unknown Gram-Schmidt variant %r" % gram_schmidt)
         self.N = problem.N
         self.nthreads = nthreads
 

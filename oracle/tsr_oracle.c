@@ -327,6 +327,9 @@ typedef struct oracle_problem {
     const double* cache_u;
     double cache_t;
     int cache_valid;
+    /* Gram-Schmidt of the Arnoldi step: 0 modified (MGS), 1 classical
+     * twice (CGS2) */
+    int gs_variant;
 } oracle_problem;
 
 oracle_problem* oracle_create(const user_data_struct* ud, const tsr_model_ext* ext)
@@ -998,6 +1001,41 @@ static void combine(const oracle_problem* P, const double* u, const double* c, i
     }
 }
 
+/* Classical Gram-Schmidt twice (CGS2) of w against v_0..v_j: the
+ * projections of w on every basis vector at once, w -= V c, the same again
+ * with the projections d of the result, H(i, j) = c_i + d_i.  Every dot is
+ * a fixed-order reduction (oracle_dot) and every update applies the basis
+ * vectors in ascending order, one fused multiply-add each.  Two passes of
+ * classical Gram-Schmidt keep the basis orthogonal to working accuracy
+ * (Giraud, Langou, Rozloznik, Comput. Math. Appl. 50 (2005) 1069-1075,
+ * "twice is enough"), with two global reductions of j+1 values instead of
+ * the j+1 sequential ones of modified Gram-Schmidt. */
+static void gs_cgs2(oracle_problem* P, int j, double* Hcol)
+{
+    const long N = P->N;
+    const double* V = P->V;
+    double* w = P->w;
+    double c[512], d[512];
+    for (int pass = 0; pass < 2; ++pass) {
+        double* h = pass == 0 ? c : d;
+        for (int i = 0; i <= j; ++i) h[i] = oracle_dot(w, V + (size_t)i * N, N);
+#pragma omp parallel for num_threads(o_threads) schedule(static) if (o_threads > 1)
+        for (long l = 0; l < N; ++l) {
+            double y = w[l];
+            for (int i = 0; i <= j; ++i) y = fma(-h[i], V[(size_t)i * N + l], y);
+            w[l] = y;
+        }
+    }
+    for (int i = 0; i <= j; ++i) Hcol[i] = c[i] + d[i];
+}
+
+int oracle_set_gram_schmidt(oracle_problem* P, int variant)
+{
+    if (!P || variant < 0 || variant > 1) return 1;
+    P->gs_variant = variant;
+    return 0;
+}
+
 #define KRYLOV_TOL 0.1
 
 int oracle_exprem_step(oracle_problem* P, double* t_io, double tend, const double* tspan,
@@ -1057,13 +1095,18 @@ int oracle_exprem_step(oracle_problem* P, double* t_io, double tend, const doubl
             oracle_jv(P, u, P->g0, vj, eps, P->w, nthreads);
             st->FuncEvals++;
             double hs = 0.0;
-            for (int i = 0; i <= j; ++i) {
-                double* vi = V + (size_t)i * N;
-                double hij = oracle_dot(P->w, vi, N);
-                Hm[(size_t)j * ldH + i] = hij;
-                hs = fma(hij, hij, hs);
+            if (P->gs_variant == 1) {
+                gs_cgs2(P, j, Hm + (size_t)j * ldH);
+                for (int i = 0; i <= j; ++i) hs = fma(Hm[(size_t)j * ldH + i], Hm[(size_t)j * ldH + i], hs);
+            } else {
+                for (int i = 0; i <= j; ++i) {
+                    double* vi = V + (size_t)i * N;
+                    double hij = oracle_dot(P->w, vi, N);
+                    Hm[(size_t)j * ldH + i] = hij;
+                    hs = fma(hij, hij, hs);
 #pragma omp parallel for num_threads(o_threads) schedule(static) if (o_threads > 1)
-                for (long l = 0; l < N; ++l) P->w[l] = fma(-hij, vi[l], P->w[l]);
+                    for (long l = 0; l < N; ++l) P->w[l] = fma(-hij, vi[l], P->w[l]);
+                }
             }
             double hn = sqrt(oracle_dot(P->w, P->w, N));
             Hm[(size_t)j * ldH + j + 1] = hn;

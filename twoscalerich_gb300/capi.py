@@ -149,6 +149,7 @@ _SIGNATURES = {
     "tsr_kernel_launches": (C.c_ulonglong, []),
     "tsr_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     "tsr_set_fused_gs": (C.c_int, [C.c_void_p, C.c_int]),
+    "tsr_set_gram_schmidt": (C.c_int, [C.c_void_p, C.c_int]),
     "tsr_set_calibrated_output": (C.c_int, [C.c_void_p, C.c_int]),
     "tsr_step_diagnostics": (C.c_int, [C.c_void_p, C.c_int, dp]),
     "tsr_cell_plan": (C.c_int, [C.c_void_p, ip]),

@@ -122,6 +122,11 @@ struct tsr_ctx {
     bool fused_gs = true;
     int gs_grid = 0;
     long long pstride = 0;
+    // Gram-Schmidt variant: 0 modified (MGS), 1 classical twice (CGS2, its
+    // own fused kernel and partial buffers for j+1 dots per pass)
+    int gs_variant = 0;
+    int gs2_grid = 0;
+    double* d_gs2part = nullptr;
     unsigned int* d_gsbar = nullptr;
     int* d_gserr = nullptr;
     std::vector<cudaGraphExec_t> graphs;
@@ -1200,7 +1205,26 @@ void arnoldi_kernels(tsr_ctx* c, int j, cudaEvent_t* ev, double frac)
         prof_end(c, pe);
         pe = prof_begin(c, 1, frac * 8.0 * (double)N * (double)(j + 3));   // algorithmic minimum
     }
-    if (c->fused_gs) {
+    if (c->gs_variant == 1) {
+        GsArgs A{};
+        A.w = c->d_w;
+        A.V = V;
+        A.ldV = N;
+        A.Hc = Hc;
+        A.hsq = scal_slot(c, S_HSQ);
+        A.ih = scal_slot(c, S_IH);
+        A.sv = scal_slot(c, S_COUNT + j);
+        A.stride = HS;
+        A.j = j;
+        A.winv = c->d_winv;
+        A.partials = c->d_gs2part;
+        A.pstride = c->pstride;
+        A.parstride = (long long)(c->maxk + 1) * c->pstride;
+        A.bar = c->d_gsbar;
+        A.err = c->d_gserr;
+        cudaMemsetAsync(c->d_gsbar, 0, 2 * sizeof(unsigned int), s);
+        launch_gs_cgs2(g, A, c->gs2_grid, s);
+    } else if (c->fused_gs) {
         GsArgs A{};
         A.w = c->d_w;
         A.V = V;
@@ -1394,7 +1418,7 @@ int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
                                 // capture the separate Gram-Schmidt kernels
                                 ge = nullptr;
                                 cudaGetLastError();
-                                if (!c->fused_gs || attempt == 1) CK(ce);
+                                if (!c->fused_gs || attempt == 1 || c->gs_variant == 1) CK(ce);
                                 c->fused_gs = false;
                                 for (auto& x : c->graphs)
                                     if (x) {
@@ -1405,7 +1429,7 @@ int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
                         }
                     }
                     CK(cudaGraphLaunch(ge, s));
-                    add_launches(c->fused_gs ? 3 : jj + 6);
+                    add_launches((c->fused_gs || c->gs_variant == 1) ? 3 : jj + 6);
                 } else {
                     arnoldi_kernels(c, jj, nullptr, frac);
                 }
@@ -1420,7 +1444,7 @@ int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
                                  sizeof(double) * HS, sizeof(double) * (size_t)nb, (size_t)S,
                                  cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
-            if (c->fused_gs) {
+            if (c->fused_gs || c->gs_variant == 1) {
                 int e = 0;
                 CK(cudaMemcpy(&e, c->d_gserr, sizeof(int), cudaMemcpyDeviceToHost));
                 if (e) {
@@ -1996,6 +2020,36 @@ extern "C" int tsr_calibrate_device(tsr_ctx* c, double* d_x)
     if (rc) return rc;
     launch_calibrate(c->P, d_x, c->stream);
     CK(cudaGetLastError());
+    return TSR_OK;
+}
+
+extern "C" int tsr_set_gram_schmidt(tsr_ctx* c, int variant)
+{
+    if (!c || variant < 0 || variant > 1) return TSR_ERR_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    if (variant == 1) {
+        if (c->maxk > gs_cgs2_max_dim()) {
+            set_error("tsr_set_gram_schmidt: classical Gram-Schmidt twice takes Krylov dimensions up to 63");
+            return TSR_ERR_ARG;
+        }
+        if (c->gs2_grid < 1) c->gs2_grid = gs_cgs2_grid(c->nsm, c->maxk);
+        if (c->gs2_grid < 1) {
+            set_error("tsr_set_gram_schmidt: the CGS2 kernel cannot be launched on this device");
+            return TSR_ERR_CUDA;
+        }
+        if (!c->d_gs2part) {
+            void* p = nullptr;
+            int rc = dev_alloc(c, sizeof(double) * 2 * (size_t)(c->maxk + 1) * (size_t)c->pstride, &p);
+            if (rc) return rc;
+            c->d_gs2part = (double*)p;
+        }
+    }
+    c->gs_variant = variant;
+    for (auto& g : c->graphs)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
     return TSR_OK;
 }
 

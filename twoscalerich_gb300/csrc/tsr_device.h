@@ -197,8 +197,9 @@ struct GsArgs {
     int stride;
     int j;
     const double* winv;
-    double* partials;           // 2 x pstride
+    double* partials;           // 2 x pstride (MGS); 2 x parstride (CGS2)
     long long pstride;
+    long long parstride;        // CGS2: distance of the two partial buffers
     unsigned int* bar;          // [2] barrier count and generation
     int* err;                   // set if a barrier wait expired
 };
@@ -207,6 +208,11 @@ int gs_fused_grid(int nsm);     // co-resident CTAs of the fused kernel
 // arrives); *timed_out = 1 if the wait expired and raised its flag
 int barrier_probe(int* timed_out);
 cudaError_t launch_gs_fused(const SegInfo& g, const GsArgs& A, int max_grid, cudaStream_t s);
+// classical Gram-Schmidt twice: co-resident CTAs for bases up to maxk + 1
+// vectors (0: cannot launch), the largest Krylov dimension it takes, launch
+int gs_cgs2_grid(int nsm, int maxk);
+int gs_cgs2_max_dim();
+cudaError_t launch_gs_cgs2(const SegInfo& g, const GsArgs& A, int nsm, cudaStream_t s);
 
 // b = a and d = c on the active segments
 void launch_seg_copy2(const double* a, double* b, const double* c, double* d, const SegInfo& g,

@@ -1220,6 +1220,263 @@ cudaError_t launch_gs_fused(const SegInfo& g, const GsArgs& A, int max_grid, cud
     return cudaLaunchKernelEx(&cfg, k_gs_fused<false>, g, A);
 }
 
+// ---- classical Gram-Schmidt twice (CGS2), fused --------------------------------
+// The Gram-Schmidt block of an Arnoldi step as two classical passes:
+//   pass 0: c_q = <w, v_q> for every q <= j at once
+//   pass 1: w -= sum_q c_q v_q (q ascending, one FMA each); d_q = <w, v_q>
+//   pass 2: w -= sum_q d_q v_q; H(q, j) = c_q + d_q; <w, w>
+//   pass 3: H(j+1, j) = sqrt, v_{j+1} = w / H(j+1, j), weighted norm
+// Every dot is formed as k_reduce forms one (same thread mapping, same
+// trees, same segment totals), so each equals a separate fixed-order
+// reduction bit for bit.  Four grid-wide (or cluster-wide) barriers per
+// Arnoldi step instead of j+3, and 3j+10 vector passes of memory traffic
+// instead of 4j+8.  Items are taken one at a time (the thread's 32 items
+// of the chunk in ascending order) with the j+1 running dot sums in
+// registers (NV >= j+1 of them, a multiple of 8), so pass 1 reads each
+// basis entry from memory once and again at once from L1.  The partials of
+// the j+1 dots of a pass sit at partials + parity * parstride + q * pstride
+// + chunk.  Dynamic shared memory: 9 NV doubles (warp sums and totals).
+constexpr int kCgs2MaxNV = 64;
+
+template <bool CLUSTER, int NV>
+__global__ void __launch_bounds__(kRedThreads) k_gs_cgs2(SegInfo g, GsArgs A)
+{
+    constexpr int Q = kRedChunk / kRedThreads;
+    extern __shared__ double sm2[];
+    const int j = A.j;
+    const int nv = j + 1;
+    double* ws = sm2;                 // [NV][8] warp sums
+    double* tot = sm2 + 8 * NV;       // [NV] segment totals of the previous pass
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    auto warp_put = [&](int q, double a) {
+#pragma unroll
+        for (int d = 16; d >= 1; d >>= 1) a = a + __shfl_xor_sync(0xffffffffu, a, d);
+        if (lane == 0) ws[8 * q + warp] = a;
+    };
+    // the chunk partials of n values: the eight warps' tree on thread q
+    auto emit = [&](int n, double* part, int b) {
+        __syncthreads();
+        if ((int)threadIdx.x < n) {
+            const double* s = ws + 8 * threadIdx.x;
+            part[(size_t)threadIdx.x * A.pstride + b] = ((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7]));
+        }
+        __syncthreads();
+    };
+    for (int p = 0; p <= 3; ++p) {
+        double* part = A.partials + (size_t)(p & 1) * A.parstride;
+        const double* prev = A.partials + (size_t)((p + 1) & 1) * A.parstride;
+        const int ntot = (p == 0) ? 0 : (p <= 2 ? nv : 1);     // values of the previous pass
+        int cs = -1;
+        for (int b = blockIdx.x; b < g.nblocks; b += gridDim.x) {
+            const SegBlock B = seg_block_at(g, b);
+            if (g.active && !g.active[B.s]) continue;
+            const long long so = (long long)B.s * A.stride;
+            const bool writer = (b == B.b0) && threadIdx.x == 0;
+            if (ntot > 0 && B.s != cs) {
+                // totals of the previous pass for this segment (segment_total's order)
+                for (int q = 0; q < ntot; ++q) {
+                    double a = 0.0;
+                    for (int i = threadIdx.x; i < B.nb; i += kRedThreads)
+                        a = a + __ldcg(prev + (size_t)q * A.pstride + B.b0 + i);
+                    warp_put(q, a);
+                }
+                __syncthreads();
+                if ((int)threadIdx.x < ntot) {
+                    const double* s = ws + 8 * threadIdx.x;
+                    tot[threadIdx.x] = ((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7]));
+                }
+                __syncthreads();
+                cs = B.s;
+            }
+            const long long base = B.lo + (long long)B.lb * kRedChunk + threadIdx.x;
+            if (p <= 1) {
+                if (p == 1 && writer)
+                    for (int q = 0; q < nv; ++q) A.Hc[so + q] = tot[q];
+                double acc[NV];
+#pragma unroll
+                for (int q = 0; q < NV; ++q) acc[q] = 0.0;
+                for (int k = 0; k < Q; ++k) {
+                    const long long i = base + (long long)k * kRedThreads;
+                    if (i >= B.hi) break;
+                    double y = A.w[i];
+                    if (p == 1) {
+                        // w -= sum_q c_q v_q, q ascending
+#pragma unroll
+                        for (int q = 0; q < NV; ++q)
+                            if (q < nv) y = fma(-tot[q], A.V[(size_t)q * A.ldV + i], y);
+                        A.w[i] = y;
+                    }
+#pragma unroll
+                    for (int q = 0; q < NV; ++q)
+                        if (q < nv) acc[q] = fma(y, A.V[(size_t)q * A.ldV + i], acc[q]);
+                }
+#pragma unroll
+                for (int q = 0; q < NV; ++q)
+                    if (q < nv) warp_put(q, acc[q]);
+                emit(nv, part, b);
+            } else if (p == 2) {
+                // w -= sum_q d_q v_q; H(q, j) = c_q + d_q; <w, w>
+                if (writer)
+                    for (int q = 0; q < nv; ++q) A.Hc[so + q] = A.Hc[so + q] + tot[q];
+                double a = 0.0;
+                for (int k = 0; k < Q; ++k) {
+                    const long long i = base + (long long)k * kRedThreads;
+                    if (i >= B.hi) break;
+                    double y = A.w[i];
+#pragma unroll
+                    for (int q = 0; q < NV; ++q)
+                        if (q < nv) y = fma(-tot[q], A.V[(size_t)q * A.ldV + i], y);
+                    A.w[i] = y;
+                    a = fma(y, y, a);
+                }
+                warp_put(0, a);
+                emit(1, part, b);
+            } else {
+                // H(j+1, j) = sqrt(<w, w>), v_{j+1} = w / H(j+1, j), weighted norm
+                const double h = tot[0];
+                const double hn = sqrt(h);
+                const double ih = 1.0 / hn;
+                if (writer) {
+                    A.hsq[so] = h;
+                    A.Hc[so + j + 1] = hn;
+                    A.ih[so] = ih;
+                }
+                double* v = A.V + (size_t)(j + 1) * A.ldV;
+                double a = 0.0;
+                for (int k = 0; k < Q; ++k) {
+                    const long long i = base + (long long)k * kRedThreads;
+                    if (i >= B.hi) break;
+                    const double vv = A.w[i] * ih;
+                    v[i] = vv;
+                    const double rr = vv * A.winv[i];
+                    a = fma(rr, rr, a);
+                }
+                warp_put(0, a);
+                emit(1, part, b);
+            }
+        }
+        if (CLUSTER) {
+            __threadfence();
+            asm volatile("barrier.cluster.arrive.release.aligned;\n"
+                         "barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+        } else if (!grid_barrier(A.bar, A.bar + 1, gridDim.x, A.err)) {
+            return;
+        }
+    }
+    // the weighted norm of v_{j+1} (total of the last pass)
+    __shared__ double ws8[8];
+    __shared__ double bc;
+    const double* last = A.partials + (size_t)(3 & 1) * A.parstride;
+    for (int b = blockIdx.x; b < g.nblocks; b += gridDim.x) {
+        const SegBlock B = seg_block_at(g, b);
+        if (g.active && !g.active[B.s]) continue;
+        if (b != B.b0) continue;
+        const double sv = segment_total(B, last, ws8, &bc);
+        if (threadIdx.x == 0) A.sv[(long long)B.s * A.stride] = sv;
+    }
+}
+
+namespace {
+using Cgs2Kernel = void (*)(SegInfo, GsArgs);
+template <bool CLUSTER>
+Cgs2Kernel cgs2_kernel(int nv)
+{
+    switch ((nv + 7) / 8) {
+    case 1: return k_gs_cgs2<CLUSTER, 8>;
+    case 2: return k_gs_cgs2<CLUSTER, 16>;
+    case 3: return k_gs_cgs2<CLUSTER, 24>;
+    case 4: return k_gs_cgs2<CLUSTER, 32>;
+    case 5: return k_gs_cgs2<CLUSTER, 40>;
+    case 6: return k_gs_cgs2<CLUSTER, 48>;
+    case 7: return k_gs_cgs2<CLUSTER, 56>;
+    case 8: return k_gs_cgs2<CLUSTER, 64>;
+    default: return nullptr;
+    }
+}
+size_t cgs2_smem(int nv) { return sizeof(double) * 9 * (size_t)(((nv + 7) / 8) * 8); }
+int g_cgs2_cluster_ok = 0;
+int g_cgs2_occ[kCgs2MaxNV / 8] = {};     // co-resident CTAs per SM, by basis-size bucket
+}  // namespace
+
+int gs_cgs2_max_dim() { return kCgs2MaxNV - 1; }
+
+// occupancy of every instantiation up to maxk + 1 basis vectors; nsm if all
+// of them can be launched cooperatively, 0 otherwise
+int gs_cgs2_grid(int nsm, int maxk)
+{
+    if (maxk + 1 > kCgs2MaxNV) return 0;
+    const int nb = (maxk + 1 + 7) / 8;
+    for (int k = 0; k < nb; ++k) {
+        const int nv = 8 * (k + 1);
+        int occ = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, cgs2_kernel<false>(nv), kRedThreads,
+                                                          cgs2_smem(nv)) != cudaSuccess || occ < 1) {
+            cudaGetLastError();
+            return 0;
+        }
+        g_cgs2_occ[k] = occ;
+    }
+    g_cgs2_cluster_ok = 0;
+    if (g_gs_cluster_max > 0) {
+        // every instantiation must schedule a cluster of the largest size used
+        bool ok = true;
+        for (int k = 0; k < nb && ok; ++k) {
+            const int nv = 8 * (k + 1);
+            if (cudaFuncSetAttribute(cgs2_kernel<true>(nv), cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                cudaSuccess) {
+                cudaGetLastError();
+                ok = false;
+                break;
+            }
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3((unsigned)g_gs_cluster_max);
+            cfg.blockDim = dim3(kRedThreads);
+            cfg.dynamicSmemBytes = cgs2_smem(nv);
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = (unsigned)g_gs_cluster_max;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            int ncl = 0;
+            if (cudaOccupancyMaxActiveClusters(&ncl, cgs2_kernel<true>(nv), &cfg) != cudaSuccess || ncl < 1) {
+                cudaGetLastError();
+                ok = false;
+            }
+        }
+        g_cgs2_cluster_ok = ok ? 1 : 0;
+    }
+    return nsm;
+}
+
+cudaError_t launch_gs_cgs2(const SegInfo& g, const GsArgs& A, int nsm, cudaStream_t s)
+{
+    count();
+    const int nv = A.j + 1;
+    if (nv > kCgs2MaxNV || g_cgs2_occ[(nv - 1) / 8] < 1) return cudaErrorInvalidValue;
+    cudaLaunchConfig_t cfg = {};
+    const int grid = std::min(g.nblocks, g_cgs2_occ[(nv - 1) / 8] * nsm);
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kRedThreads);
+    cfg.dynamicSmemBytes = cgs2_smem(nv);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (g_cgs2_cluster_ok && grid <= g_gs_cluster_max && grid == g.nblocks) {
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)grid;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        return cudaLaunchKernelEx(&cfg, cgs2_kernel<true>(nv), g, A);
+    }
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    return cudaLaunchKernelEx(&cfg, cgs2_kernel<false>(nv), g, A);
+}
+
 // ---- elementwise, over segments (same block mapping as the reductions) -------
 template <class Op>
 __global__ void __launch_bounds__(kRedThreads) k_segmap(Op op, SegInfo g)

@@ -495,7 +495,9 @@ def from_reference_files(options_file, keff_file="Keff.txt", macro_bc=(1, 3, 2, 
 class Context:
     """The GPU hot path of one problem (a tsr_ctx)."""
 
-    def __init__(self, problem, max_krylov=None, stream=None):
+    def __init__(self, problem, max_krylov=None, stream=None, gram_schmidt=0):
+        """gram_schmidt: 0 modified Gram-Schmidt (the reference's), 1
+        classical Gram-Schmidt twice (tsr_set_gram_schmidt)."""
         self.lib = capi.load()
         self.p = problem
         mk = problem.options.MaxKrylov if max_krylov is None else max_krylov
@@ -504,6 +506,8 @@ class Context:
             raise capi.TsrError(1, "tsr_init")
         self.h = h
         self.N = problem.N
+        if gram_schmidt:
+            check(self.lib.tsr_set_gram_schmidt(h, gram_schmidt), "tsr_set_gram_schmidt")
 
     def g(self, u):
         out = np.empty(self.N)
