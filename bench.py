@@ -714,6 +714,7 @@ def run_to_end_bench(args):
         return
     p = P.config1()
     ctx = P.Context(p, gram_schmidt=GS[args.gs])
+    tuned = ctx.autotune(p.u0, reps=5)               # the cell kernel's plan for this size
     for _ in range(args.warmup):                      # warm: one full run
         P.run_to_end(ctx.exprem_step, p)
     clocks = Clocks()
@@ -749,6 +750,8 @@ def run_to_end_bench(args):
         "speedup_vs_cpu": cpu_s / gpu_s,
         "e2e": {"value": gpu_s, "unit": "s", "h2d_bytes_per_step": 8 * p.N, "d2h_bytes_per_step": 8 * p.N},
         "clocks": clk, "gpu_launches": int(launches),
+        "autotuned": dict({"g_ms": tuned[0], "threads": tuned[1], "smem_budget": tuned[2]},
+                          **cell_plan(ctx.lib, ctx.h)),
     }
     print(json.dumps(line))
 

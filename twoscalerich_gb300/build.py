@@ -56,7 +56,13 @@ def build(verbose=False, force=False):
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers += [os.path.join(HERE, "..", "include", f)
                 for f in os.listdir(os.path.join(HERE, "..", "include"))]
-    host_flags = ["-fPIC", "-O2", "-ffp-contract=off"]
+    # OpenMP: the host evaluates independent phi_1 Pade approximants of an
+    # Arnoldi batch side by side
+    host_flags = ["-fPIC", "-O2", "-ffp-contract=off", "-fopenmp"]
+    if platform.machine() == "x86_64":
+        # fma() as the hardware instruction (a library call otherwise); the
+        # results are the same either way, fma rounds once
+        host_flags.append("-mfma")
     jobs = []
     objs = []
     for src in CU_SOURCES:
@@ -84,7 +90,7 @@ def build(verbose=False, force=False):
         for o in outs:
             sys.stdout.write(o)
     if force or jobs or not os.path.exists(LIB):
-        _run([nvcc, "-shared", "-o", LIB] + objs + ["-cudart", "static"] + ARCH)
+        _run([nvcc, "-shared", "-o", LIB] + objs + ["-cudart", "static", "-lgomp"] + ARCH)
     return LIB
 
 

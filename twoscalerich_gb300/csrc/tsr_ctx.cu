@@ -48,6 +48,8 @@ struct ScenState {
     int m = 0, maxk = 0;
     int m_prev = 0;              // Krylov dimension of the last accepted step
     std::vector<double> Hm, phi, cv, z;
+    int phi_m = 0;               // phi holds phi_1(phi_alpha H_m) for m = phi_m (0: nothing)
+    double phi_alpha = 0.0;
     // what limited the last accepted step: its proposed size, the number of
     // halvings because the Krylov space was too small at the largest
     // dimension, the rejected attempts, the error of the accepted attempt,
@@ -1175,7 +1177,59 @@ int phi_host(tsr_ctx* c, ScenState& z, double alpha, int m)
 {
     int rc = phipade_host(z.phi.data(), z.Hm.data(), alpha, m, c->ldH, c->maxk);
     if (rc) set_error("phipade: singular Pade denominator");
+    z.phi_m = rc ? 0 : m;
+    z.phi_alpha = alpha;
     return rc;
+}
+
+// phi_1(dt H_m) for the Krylov dimensions that the column tests of one
+// batch of Arnoldi steps may reach, each scenario up to its happy breakdown
+// or its largest dimension.  They are independent, so they are evaluated
+// side by side on the host's threads (phipade_host is re-entrant); each is
+// the value phi_host would give, and the tests take them in their
+// sequential order.
+struct PhiJob {
+    int q, m, rc;
+    size_t off;
+};
+
+void phi_batch(tsr_ctx* c, const std::vector<int>& arn, int j, int nb, size_t row, int min_krylov,
+               std::vector<PhiJob>& jobs, std::vector<int>& slot, std::vector<double>& buf)
+{
+    jobs.clear();
+    slot.assign((size_t)c->S * (size_t)nb, -1);     // (scenario, m - 1 - j) -> job
+    const int ldH = c->ldH;
+    const size_t blk = (size_t)c->maxk * (size_t)c->maxk;
+    for (int q = 0; q < c->S; ++q) {
+        if (!arn[q]) continue;
+        ScenState& z = c->sc[q];
+        for (int jj = j; jj < j + nb; ++jj) {
+            const double* col = c->h_stage + (size_t)q * row + (size_t)(jj - j) * ldH;
+            double hs = 0.0;
+            for (int i = 0; i <= jj; ++i) {
+                z.Hm[(size_t)jj * ldH + i] = col[i];
+                hs = std::fma(col[i], col[i], hs);
+            }
+            const double hn = col[jj + 1];
+            z.Hm[(size_t)jj * ldH + jj + 1] = hn;
+            const int m = jj + 1;
+            if (!(hn > 1e-12 * std::sqrt(std::fma(hn, hn, hs)))) break;
+            if (!(m < min_krylov && m < z.maxk)) {
+                slot[(size_t)q * nb + (size_t)(jj - j)] = (int)jobs.size();
+                jobs.push_back({q, m, 0, 0});
+            }
+            if (m >= z.maxk) break;
+        }
+    }
+    for (size_t k = 0; k < jobs.size(); ++k) jobs[k].off = k * blk;
+    if (buf.size() < jobs.size() * blk) buf.resize(jobs.size() * blk);
+    const long n = (long)jobs.size();
+#pragma omp parallel for schedule(dynamic, 1) if (n > 1)
+    for (long k = n - 1; k >= 0; --k) {          // largest dimensions first
+        PhiJob& J = jobs[(size_t)k];
+        ScenState& z = c->sc[J.q];
+        J.rc = phipade_host(buf.data() + J.off, z.Hm.data(), z.dt, J.m, c->ldH, c->maxk);
+    }
 }
 
 // The kernels of Arnoldi step j for every active scenario: w = J v_j
@@ -1268,6 +1322,9 @@ struct RoundIO {
 // records its status and leaves the round; a CUDA error ends the round.
 int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
 {
+    thread_local std::vector<PhiJob> phi_jobs;
+    thread_local std::vector<int> phi_slot;
+    thread_local std::vector<double> phi_buf;
     const int S = c->S;
     const exprem_options_struct* opt = io.opt;
     cudaStream_t s = c->stream;
@@ -1363,6 +1420,7 @@ int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
     for (int q : live) {
         ScenState& z = c->sc[q];
         std::fill(z.Hm.begin(), z.Hm.end(), 0.0);
+        z.phi_m = 0;
         z.beta = std::sqrt(c->h_stage[2 * q]);
         z.nu = std::sqrt(c->h_stage[2 * q + 1]);
         z.eps = std::sqrt((1.0 + z.nu) * DBL_EPSILON);
@@ -1453,6 +1511,7 @@ int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
                     return TSR_ERR_TIMEOUT;
                 }
             }
+            phi_batch(c, arn, j, nb, row, opt->MinKrylov, phi_jobs, phi_slot, phi_buf);
             for (int jj = j; jj < j + nb && narn > 0; ++jj) {
                 if (c->use_graphs && c->prof) {
                     std::array<cudaEvent_t, 4>& ev = c->graph_ev[(size_t)jj];
@@ -1486,7 +1545,25 @@ int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
                         stop = true;
                     } else if (!(z.m < opt->MinKrylov && z.m < z.maxk)) {
                         z.vnw = std::sqrt(Sv / (double)Ns(q));
-                        if ((rc = phi_host(c, z, z.dt, z.m))) {
+                        // the batch's evaluation of phi_1(dt H_m) for this scenario and m
+                        const int jb = phi_slot[(size_t)q * nb + (size_t)(jj - j)];
+                        if (jb < 0) {
+                            set_error("internal: phi_1 evaluation missing from the batch");
+                            return TSR_ERR_ARG;
+                        }
+                        const PhiJob& J = phi_jobs[(size_t)jb];
+                        rc = J.rc;
+                        if (rc) {
+                            set_error("phipade: singular Pade denominator");
+                            z.phi_m = 0;
+                        } else {
+                            for (int cc = 0; cc < z.m; ++cc)
+                                std::memcpy(z.phi.data() + (size_t)cc * c->maxk,
+                                            phi_buf.data() + J.off + (size_t)cc * c->maxk, sizeof(double) * z.m);
+                            z.phi_m = z.m;
+                            z.phi_alpha = z.dt;
+                        }
+                        if (rc) {
                             fail(q, rc, "phipade: singular Pade denominator");
                             stop = true;
                         } else {
@@ -1539,7 +1616,8 @@ int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
             const int m = z.m;
             int mz = 0;
             if (m > 0) {
-                if ((rc = phi_host(c, z, z.dt, m))) {
+                // phi_1(dt H_m) from the Krylov tests when dt is still theirs
+                if (!(z.phi_m == m && z.phi_alpha == z.dt) && (rc = phi_host(c, z, z.dt, m))) {
                     fail(q, rc, "phipade: singular Pade denominator");
                     continue;
                 }

@@ -21,6 +21,7 @@
 //     vertex j+1's.
 //   * interpolant coefficients: triangles h = a0 x + a1 y + a2, quadrilaterals
 //     h = a0 x + a1 y + a2 xy + a3, from the inverse of the vertex matrix.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -575,14 +576,51 @@ extern "C" int tsr_set_exprem_options(exprem_options_struct* o)
 
 namespace tsr {
 
+// C = A B: element (i, j) is the chain c = fma(A(i, k), B(k, j), c), k
+// ascending.  Eight (then four, then one) elements of a column are formed
+// side by side, each by its own chain in that order, so the FMA latency is
+// hidden without changing a single rounding.
 static void matmul(int m, const double* A, const double* B, double* C)
 {
-    for (int j = 0; j < m; ++j)
-        for (int i = 0; i < m; ++i) {
-            double c = 0.0;
-            for (int k = 0; k < m; ++k) c = std::fma(A[k * m + i], B[j * m + k], c);
-            C[j * m + i] = c;
+    for (int j = 0; j < m; ++j) {
+        const double* b = B + (size_t)j * m;
+        double* c = C + (size_t)j * m;
+        int i = 0;
+        for (; i + 8 <= m; i += 8) {
+            double c0 = 0.0, c1 = 0.0, c2 = 0.0, c3 = 0.0, c4 = 0.0, c5 = 0.0, c6 = 0.0, c7 = 0.0;
+            for (int k = 0; k < m; ++k) {
+                const double bk = b[k];
+                const double* a = A + (size_t)k * m + i;
+                c0 = std::fma(a[0], bk, c0);
+                c1 = std::fma(a[1], bk, c1);
+                c2 = std::fma(a[2], bk, c2);
+                c3 = std::fma(a[3], bk, c3);
+                c4 = std::fma(a[4], bk, c4);
+                c5 = std::fma(a[5], bk, c5);
+                c6 = std::fma(a[6], bk, c6);
+                c7 = std::fma(a[7], bk, c7);
+            }
+            c[i] = c0; c[i + 1] = c1; c[i + 2] = c2; c[i + 3] = c3;
+            c[i + 4] = c4; c[i + 5] = c5; c[i + 6] = c6; c[i + 7] = c7;
         }
+        for (; i + 4 <= m; i += 4) {
+            double c0 = 0.0, c1 = 0.0, c2 = 0.0, c3 = 0.0;
+            for (int k = 0; k < m; ++k) {
+                const double bk = b[k];
+                const double* a = A + (size_t)k * m + i;
+                c0 = std::fma(a[0], bk, c0);
+                c1 = std::fma(a[1], bk, c1);
+                c2 = std::fma(a[2], bk, c2);
+                c3 = std::fma(a[3], bk, c3);
+            }
+            c[i] = c0; c[i + 1] = c1; c[i + 2] = c2; c[i + 3] = c3;
+        }
+        for (; i < m; ++i) {
+            double cc = 0.0;
+            for (int k = 0; k < m; ++k) cc = std::fma(A[(size_t)k * m + i], b[k], cc);
+            c[i] = cc;
+        }
+    }
 }
 
 int phipade_host(double* phiH, const double* H, double alpha, int m, int ldH, int ldP)
@@ -605,7 +643,15 @@ int phipade_host(double* phiH, const double* H, double alpha, int m, int ldH, in
     static const double b[6] = {-6.0 / 13.0, 5.0 / 52.0, -5.0 / 429.0,
                                 1.0 / 1144.0, -1.0 / 25740.0, 1.0 / 1235520.0};
     const int mm = m * m;
-    std::vector<double> A(mm), P(mm), D(mm), F(mm), E(mm), T(mm);
+    // work matrices, kept per thread between calls
+    thread_local std::vector<double> work;
+    if (work.size() < (size_t)6 * mm) work.resize((size_t)6 * mm);
+    double* A = work.data();
+    double* P = A + mm;
+    double* D = P + mm;
+    double* F = D + mm;
+    double* E = F + mm;
+    double* T = E + mm;
     for (int j = 0; j < m; ++j)
         for (int i = 0; i < m; ++i) A[j * m + i] = alpha * H[j * ldH + i];
     double nrm = 0.0;
@@ -630,14 +676,14 @@ int phipade_host(double* phiH, const double* H, double alpha, int m, int ldH, in
             D[j * m + i] = d;
             E[j * m + i] = d;
         }
-    P = A;
+    std::copy(A, A + mm, P);
     for (int i = 0; i < mm; ++i) {
         F[i] = std::fma(a[0], P[i], F[i]);
         D[i] = std::fma(b[0], P[i], D[i]);
     }
     for (int p = 1; p < 6; ++p) {
-        matmul(m, P.data(), A.data(), T.data());
-        P = T;
+        matmul(m, P, A, T);
+        std::swap(P, T);
         for (int i = 0; i < mm; ++i) {
             F[i] = std::fma(a[p], P[i], F[i]);
             D[i] = std::fma(b[p], P[i], D[i]);
@@ -671,14 +717,14 @@ int phipade_host(double* phiH, const double* H, double alpha, int m, int ldH, in
             F[j * m + i] = s / D[i * m + i];
         }
     if (scale > 0) {
-        matmul(m, A.data(), F.data(), T.data());           // E = A phi + I
+        matmul(m, A, F, T);                                // E = A phi + I
         for (int i = 0; i < mm; ++i) E[i] += T[i];
         for (int it = 0; it < scale; ++it) {
             if (it > 0) {
-                matmul(m, E.data(), E.data(), T.data());   // E = E^2
-                E = T;
+                matmul(m, E, E, T);                        // E = E^2
+                std::swap(E, T);
             }
-            matmul(m, E.data(), F.data(), T.data());       // phi = (E phi + phi) / 2
+            matmul(m, E, F, T);                            // phi = (E phi + phi) / 2
             for (int i = 0; i < mm; ++i) F[i] = 0.5 * (T[i] + F[i]);
         }
     }
