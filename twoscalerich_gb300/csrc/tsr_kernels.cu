@@ -1290,26 +1290,50 @@ __global__ void __launch_bounds__(kRedThreads) k_gs_cgs2(SegInfo g, GsArgs A)
                 cs = B.s;
             }
             const long long base = B.lo + (long long)B.lb * kRedChunk + threadIdx.x;
+            // items in groups of KG (ascending), so that KG loads of every
+            // basis vector are in flight at once; per value the sums still
+            // run over the items in ascending order
+            constexpr int KG = 4;
             if (p <= 1) {
                 if (p == 1 && writer)
                     for (int q = 0; q < nv; ++q) A.Hc[so + q] = tot[q];
                 double acc[NV];
 #pragma unroll
                 for (int q = 0; q < NV; ++q) acc[q] = 0.0;
-                for (int k = 0; k < Q; ++k) {
-                    const long long i = base + (long long)k * kRedThreads;
-                    if (i >= B.hi) break;
-                    double y = A.w[i];
+                for (int k0 = 0; k0 < Q; k0 += KG) {
+                    if (base + (long long)k0 * kRedThreads >= B.hi) break;
+                    long long ii[KG];
+                    bool in[KG];
+                    double y[KG];
+#pragma unroll
+                    for (int u = 0; u < KG; ++u) {
+                        ii[u] = base + (long long)(k0 + u) * kRedThreads;
+                        in[u] = ii[u] < B.hi;
+                        y[u] = in[u] ? A.w[ii[u]] : 0.0;
+                    }
                     if (p == 1) {
                         // w -= sum_q c_q v_q, q ascending
 #pragma unroll
-                        for (int q = 0; q < NV; ++q)
-                            if (q < nv) y = fma(-tot[q], A.V[(size_t)q * A.ldV + i], y);
-                        A.w[i] = y;
+                        for (int q = 0; q < NV; ++q) {
+                            if (q >= nv) break;
+                            const double h = tot[q];
+                            const double* vq = A.V + (size_t)q * A.ldV;
+#pragma unroll
+                            for (int u = 0; u < KG; ++u)
+                                if (in[u]) y[u] = fma(-h, vq[ii[u]], y[u]);
+                        }
+#pragma unroll
+                        for (int u = 0; u < KG; ++u)
+                            if (in[u]) A.w[ii[u]] = y[u];
                     }
 #pragma unroll
-                    for (int q = 0; q < NV; ++q)
-                        if (q < nv) acc[q] = fma(y, A.V[(size_t)q * A.ldV + i], acc[q]);
+                    for (int q = 0; q < NV; ++q) {
+                        if (q >= nv) break;
+                        const double* vq = A.V + (size_t)q * A.ldV;
+#pragma unroll
+                        for (int u = 0; u < KG; ++u)
+                            if (in[u]) acc[q] = fma(y[u], vq[ii[u]], acc[q]);
+                    }
                 }
 #pragma unroll
                 for (int q = 0; q < NV; ++q)
@@ -1320,15 +1344,32 @@ __global__ void __launch_bounds__(kRedThreads) k_gs_cgs2(SegInfo g, GsArgs A)
                 if (writer)
                     for (int q = 0; q < nv; ++q) A.Hc[so + q] = A.Hc[so + q] + tot[q];
                 double a = 0.0;
-                for (int k = 0; k < Q; ++k) {
-                    const long long i = base + (long long)k * kRedThreads;
-                    if (i >= B.hi) break;
-                    double y = A.w[i];
+                for (int k0 = 0; k0 < Q; k0 += KG) {
+                    if (base + (long long)k0 * kRedThreads >= B.hi) break;
+                    long long ii[KG];
+                    bool in[KG];
+                    double y[KG];
 #pragma unroll
-                    for (int q = 0; q < NV; ++q)
-                        if (q < nv) y = fma(-tot[q], A.V[(size_t)q * A.ldV + i], y);
-                    A.w[i] = y;
-                    a = fma(y, y, a);
+                    for (int u = 0; u < KG; ++u) {
+                        ii[u] = base + (long long)(k0 + u) * kRedThreads;
+                        in[u] = ii[u] < B.hi;
+                        y[u] = in[u] ? A.w[ii[u]] : 0.0;
+                    }
+#pragma unroll
+                    for (int q = 0; q < NV; ++q) {
+                        if (q >= nv) break;
+                        const double h = tot[q];
+                        const double* vq = A.V + (size_t)q * A.ldV;
+#pragma unroll
+                        for (int u = 0; u < KG; ++u)
+                            if (in[u]) y[u] = fma(-h, vq[ii[u]], y[u]);
+                    }
+#pragma unroll
+                    for (int u = 0; u < KG; ++u)
+                        if (in[u]) {
+                            A.w[ii[u]] = y[u];
+                            a = fma(y[u], y[u], a);
+                        }
                 }
                 warp_put(0, a);
                 emit(1, part, b);
@@ -1344,13 +1385,15 @@ __global__ void __launch_bounds__(kRedThreads) k_gs_cgs2(SegInfo g, GsArgs A)
                 }
                 double* v = A.V + (size_t)(j + 1) * A.ldV;
                 double a = 0.0;
+#pragma unroll 8
                 for (int k = 0; k < Q; ++k) {
                     const long long i = base + (long long)k * kRedThreads;
-                    if (i >= B.hi) break;
-                    const double vv = A.w[i] * ih;
-                    v[i] = vv;
-                    const double rr = vv * A.winv[i];
-                    a = fma(rr, rr, a);
+                    if (i < B.hi) {
+                        const double vv = A.w[i] * ih;
+                        v[i] = vv;
+                        const double rr = vv * A.winv[i];
+                        a = fma(rr, rr, a);
+                    }
                 }
                 warp_put(0, a);
                 emit(1, part, b);
