@@ -1194,6 +1194,12 @@ int gs_fused_grid(int nsm)
     return occ * nsm;
 }
 
+bool gs_fused_is_cluster(const SegInfo& g, int max_grid)
+{
+    const int grid = std::min(g.nblocks, max_grid);
+    return grid <= g_gs_cluster_max && grid == g.nblocks;
+}
+
 cudaError_t launch_gs_fused(const SegInfo& g, const GsArgs& A, int max_grid, cudaStream_t s)
 {
     count();
