@@ -131,8 +131,6 @@ struct tsr_ctx {
     double* d_gs2part = nullptr;
     unsigned int* d_gsbar = nullptr;
     int* d_gserr = nullptr;
-    int* h_gserr = nullptr;              // pinned: the barrier-error flag after each Arnoldi step
-    std::vector<cudaEvent_t> col_ev;     // one per Arnoldi index: its column is in h_stage
     std::vector<cudaGraphExec_t> graphs;
     std::vector<std::array<cudaEvent_t, 4>> graph_ev;
     double prof_acc_ms[2] = {0.0, 0.0}, prof_acc_bytes[2] = {0.0, 0.0};
@@ -815,8 +813,6 @@ int alloc_work(tsr_ctx* c, int max_krylov)
     CK(cudaMallocHost(&c->h_active, sizeof(int) * (size_t)S));
     CK(cudaMallocHost(&c->h_mint, sizeof(int) * 2 * (size_t)S));
     CK(cudaMallocHost(&c->h_stage, sizeof(double) * ((size_t)c->ldH * mk1 + mk1 + 4) * S));
-    CK(cudaMallocHost(&c->h_gserr, sizeof(int) * ((size_t)mk1 + 1)));
-    std::memset(c->h_gserr, 0, sizeof(int) * ((size_t)mk1 + 1));
     std::memset(c->h_eps, 0, sizeof(double) * 3 * (size_t)S);
     std::memset(c->h_coef, 0, sizeof(double) * (size_t)c->CS * S);
     std::memset(c->h_mint, 0, sizeof(int) * 2 * (size_t)S);
@@ -1010,9 +1006,6 @@ extern "C" void tsr_free(tsr_ctx* c)
     if (c->h_active) cudaFreeHost(c->h_active);
     if (c->h_mint) cudaFreeHost(c->h_mint);
     if (c->h_stage) cudaFreeHost(c->h_stage);
-    if (c->h_gserr) cudaFreeHost(c->h_gserr);
-    for (cudaEvent_t e : c->col_ev)
-        if (e) cudaEventDestroy(e);
     for (void* p : c->allocs) cudaFree(p);
     if (c->h_scal) cudaFreeHost(c->h_scal);
     if (c->h_coef) cudaFreeHost(c->h_coef);
@@ -1211,7 +1204,7 @@ void phi_batch(tsr_ctx* c, const std::vector<int>& arn, int j, int nb, size_t ro
         if (!arn[q]) continue;
         ScenState& z = c->sc[q];
         for (int jj = j; jj < j + nb; ++jj) {
-            const double* col = c->h_stage + (size_t)q * row + (size_t)jj * ldH;
+            const double* col = c->h_stage + (size_t)q * row + (size_t)(jj - j) * ldH;
             double hs = 0.0;
             for (int i = 0; i <= jj; ++i) {
                 z.Hm[(size_t)jj * ldH + i] = col[i];
@@ -1450,104 +1443,79 @@ int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
         if ((rc = set_active(c, arn))) return rc;
         launch_seg_scale(c->d_g0, scal_slot(c, S_IB), HS, V, c->seg, s);
         // The first batch of Arnoldi steps is launched back to back up to the
-        // smallest Krylov dimension the iterating scenarios took last time.
-        // After that one step more than has been checked is always in
-        // flight: while the host tests the columns of the steps launched so
-        // far, the GPU computes the next one.  Columns are tested in order
-        // exactly as if each had been read back alone (steps past a
-        // scenario's stopping point only write columns, basis vectors and
-        // scratch it never uses, and are not counted).  Every step's column,
-        // weighted norm and barrier-error flag are copied to fixed places of
-        // the pinned staging area behind it, and an event marks them.
+        // smallest Krylov dimension the iterating scenarios took last time;
+        // their columns are then checked in order exactly as if each had been
+        // read back alone (steps past a scenario's stopping point only write
+        // columns it never uses).  Further steps go one at a time.
         int pred = c->maxk;
-        int lim = 0;
         for (int q = 0; q < S; ++q)
-            if (arn[q]) {
-                pred = std::min(pred, std::max(1, c->sc[q].m_prev));
-                lim = std::max(lim, c->sc[q].maxk);
-            }
-        const size_t R = (size_t)c->maxk * ldH + (size_t)c->maxk;   // staging doubles per scenario
-        const bool fused = c->fused_gs || c->gs_variant == 1;
-        if (c->col_ev.size() < (size_t)c->maxk) c->col_ev.resize((size_t)c->maxk, nullptr);
-        auto launch_step = [&](int jj) -> int {
-            int rc2;
-            if ((rc2 = set_active(c, arn))) return rc2;
+            if (arn[q]) pred = std::min(pred, std::max(1, c->sc[q].m_prev));
+        int j = 0;
+        while (j < c->maxk && narn > 0) {
+            const int nb = (j == 0) ? std::max(1, std::min(pred, c->maxk)) : 1;
+            if ((rc = set_active(c, arn))) return rc;
             const double frac = (double)narn / S;
-            if (c->use_graphs) {
-                cudaGraphExec_t& ge = c->graphs[(size_t)jj];
-                std::array<cudaEvent_t, 4>& ev = c->graph_ev[(size_t)jj];
-                if (!ge) {
-                    // first use of this index: capture with nothing in flight
-                    CK(cudaStreamSynchronize(s));
-                    for (auto& e : ev)
-                        if (!e) CK(cudaEventCreate(&e));
-                    for (int attempt = 0; attempt < 2 && !ge; ++attempt) {
-                        set_counting(false);
-                        CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-                        arnoldi_kernels(c, jj, ev.data(), frac);
-                        cudaGraph_t g = nullptr;
-                        cudaError_t ce = cudaStreamEndCapture(s, &g);
-                        set_counting(true);
-                        if (ce == cudaSuccess) ce = cudaGraphInstantiate(&ge, g, 0);
-                        if (g) cudaGraphDestroy(g);
-                        if (ce != cudaSuccess) {
-                            // a cooperative launch that cannot be captured:
-                            // capture the separate Gram-Schmidt kernels
-                            ge = nullptr;
-                            cudaGetLastError();
-                            if (!c->fused_gs || attempt == 1 || c->gs_variant == 1) CK(ce);
-                            c->fused_gs = false;
-                            for (auto& x : c->graphs)
-                                if (x) {
-                                    cudaGraphExecDestroy(x);
-                                    x = nullptr;
-                                }
+            for (int jj = j; jj < j + nb; ++jj) {
+                if (c->use_graphs) {
+                    cudaGraphExec_t& ge = c->graphs[(size_t)jj];
+                    std::array<cudaEvent_t, 4>& ev = c->graph_ev[(size_t)jj];
+                    if (!ge) {
+                        for (auto& e : ev)
+                            if (!e) CK(cudaEventCreate(&e));
+                        for (int attempt = 0; attempt < 2 && !ge; ++attempt) {
+                            set_counting(false);
+                            CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+                            arnoldi_kernels(c, jj, ev.data(), frac);
+                            cudaGraph_t g = nullptr;
+                            cudaError_t ce = cudaStreamEndCapture(s, &g);
+                            set_counting(true);
+                            if (ce == cudaSuccess) ce = cudaGraphInstantiate(&ge, g, 0);
+                            if (g) cudaGraphDestroy(g);
+                            if (ce != cudaSuccess) {
+                                // a cooperative launch that cannot be captured:
+                                // capture the separate Gram-Schmidt kernels
+                                ge = nullptr;
+                                cudaGetLastError();
+                                if (!c->fused_gs || attempt == 1 || c->gs_variant == 1) CK(ce);
+                                c->fused_gs = false;
+                                for (auto& x : c->graphs)
+                                    if (x) {
+                                        cudaGraphExecDestroy(x);
+                                        x = nullptr;
+                                    }
+                            }
                         }
                     }
+                    CK(cudaGraphLaunch(ge, s));
+                    add_launches((c->fused_gs || c->gs_variant == 1) ? 3 : jj + 6);
+                } else {
+                    arnoldi_kernels(c, jj, nullptr, frac);
                 }
-                CK(cudaGraphLaunch(ge, s));
-                add_launches((c->fused_gs || c->gs_variant == 1) ? 3 : jj + 6);
-            } else {
-                arnoldi_kernels(c, jj, nullptr, frac);
             }
             CK(cudaGetLastError());
-            CK(cudaMemcpy2DAsync(c->h_stage + (size_t)jj * ldH, sizeof(double) * R, c->d_scal + (size_t)jj * ldH,
-                                 sizeof(double) * HS, sizeof(double) * (size_t)ldH, (size_t)S,
+            // columns j..j+nb-1 of every H and the weighted norms of v_{j+1..j+nb}
+            const size_t row = (size_t)nb * ldH + (size_t)nb;
+            CK(cudaMemcpy2DAsync(c->h_stage, sizeof(double) * row, c->d_scal + (size_t)j * ldH,
+                                 sizeof(double) * HS, sizeof(double) * (size_t)nb * ldH, (size_t)S,
                                  cudaMemcpyDeviceToHost, s));
-            CK(cudaMemcpy2DAsync(c->h_stage + (size_t)c->maxk * ldH + (size_t)jj, sizeof(double) * R,
-                                 scal_slot(c, S_COUNT + jj), sizeof(double) * HS, sizeof(double), (size_t)S,
+            CK(cudaMemcpy2DAsync(c->h_stage + (size_t)nb * ldH, sizeof(double) * row, scal_slot(c, S_COUNT + j),
+                                 sizeof(double) * HS, sizeof(double) * (size_t)nb, (size_t)S,
                                  cudaMemcpyDeviceToHost, s));
-            if (fused)
-                CK(cudaMemcpyAsync(c->h_gserr + jj, c->d_gserr, sizeof(int), cudaMemcpyDeviceToHost, s));
-            if (!c->col_ev[(size_t)jj]) CK(cudaEventCreateWithFlags(&c->col_ev[(size_t)jj], cudaEventDisableTiming));
-            CK(cudaEventRecord(c->col_ev[(size_t)jj], s));
-            return TSR_OK;
-        };
-        int j = 0;                               // first column not yet tested
-        int launched = lim > 0 ? std::max(1, std::min(pred, lim)) : 0;
-        for (int jj = 0; jj < launched; ++jj)
-            if ((rc = launch_step(jj))) return rc;
-        while (j < launched && narn > 0) {
-            const int nb = launched - j;         // columns j .. launched-1 are tested now
-            if (launched < lim) {                // the next step, ahead of the tests
-                if ((rc = launch_step(launched))) return rc;
-                ++launched;
+            CK(cudaStreamSynchronize(s));
+            if (c->fused_gs || c->gs_variant == 1) {
+                int e = 0;
+                CK(cudaMemcpy(&e, c->d_gserr, sizeof(int), cudaMemcpyDeviceToHost));
+                if (e) {
+                    set_error("Gram-Schmidt: a grid barrier wait expired");
+                    cudaMemset(c->d_gserr, 0, sizeof(int));
+                    return TSR_ERR_TIMEOUT;
+                }
             }
-            CK(cudaEventSynchronize(c->col_ev[(size_t)(j + nb - 1)]));
-            if (fused)
-                for (int jj = j; jj < j + nb; ++jj)
-                    if (c->h_gserr[jj]) {
-                        CK(cudaStreamSynchronize(s));
-                        set_error("Gram-Schmidt: a grid barrier wait expired");
-                        cudaMemset(c->d_gserr, 0, sizeof(int));
-                        return TSR_ERR_TIMEOUT;
-                    }
-            phi_batch(c, arn, j, nb, R, opt->MinKrylov, phi_jobs, phi_slot, phi_buf);
+            phi_batch(c, arn, j, nb, row, opt->MinKrylov, phi_jobs, phi_slot, phi_buf);
             for (int jj = j; jj < j + nb && narn > 0; ++jj) {
                 if (c->use_graphs && c->prof) {
                     std::array<cudaEvent_t, 4>& ev = c->graph_ev[(size_t)jj];
                     float ta = 0.f, tb = 0.f;
-                    const double frac = (double)narn / S;
                     CK(cudaEventElapsedTime(&ta, ev[0], ev[1]));
                     CK(cudaEventElapsedTime(&tb, ev[2], ev[3]));
                     c->prof_acc_ms[0] += ta;
@@ -1561,7 +1529,7 @@ int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
                     if (!arn[q]) continue;
                     ScenState& z = c->sc[q];
                     io.st[q].FuncEvals++;
-                    const double* col = c->h_stage + (size_t)q * R + (size_t)jj * ldH;
+                    const double* col = c->h_stage + (size_t)q * row + (size_t)(jj - j) * ldH;
                     double hs = 0.0;
                     for (int i = 0; i <= jj; ++i) {
                         z.Hm[(size_t)jj * ldH + i] = col[i];
@@ -1569,7 +1537,7 @@ int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
                     }
                     const double hn = col[jj + 1];
                     z.Hm[(size_t)jj * ldH + jj + 1] = hn;
-                    const double Sv = c->h_stage[(size_t)q * R + (size_t)c->maxk * ldH + (size_t)jj];
+                    const double Sv = c->h_stage[(size_t)q * row + (size_t)nb * ldH + (size_t)(jj - j)];
                     z.m = jj + 1;
                     bool stop = false;
                     if (!(hn > 1e-12 * std::sqrt(std::fma(hn, hn, hs)))) {
