@@ -302,7 +302,10 @@ int tsr_cell_summary(tsr_ctx* ctx, const double* u, double* out);
  * EXPREM steps; enabling clears earlier records.  Category 0: G and
  * finite-difference Jv evaluations; 1: the Gram-Schmidt block of an Arnoldi
  * step.  tsr_profile_read returns the summed device time (ms), the number
- * of timed launches and their summed algorithmic bytes. */
+ * of timed launches and their summed algorithmic bytes.  The per-index
+ * Arnoldi graphs carry their timing events only while profiling is on, so
+ * switching it on or off makes the next steps capture them again; calling
+ * it with the current setting only clears the records. */
 int tsr_profile(tsr_ctx* ctx, int enable);
 int tsr_profile_read(tsr_ctx* ctx, int category, double* ms, long long* count, double* bytes);
 

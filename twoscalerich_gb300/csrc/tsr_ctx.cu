@@ -1465,7 +1465,8 @@ int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
                         for (int attempt = 0; attempt < 2 && !ge; ++attempt) {
                             set_counting(false);
                             CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-                            arnoldi_kernels(c, jj, ev.data(), frac);
+                            // event-record nodes only while profiling
+                            arnoldi_kernels(c, jj, c->prof ? ev.data() : nullptr, frac);
                             cudaGraph_t g = nullptr;
                             cudaError_t ce = cudaStreamEndCapture(s, &g);
                             set_counting(true);
@@ -1891,6 +1892,14 @@ extern "C" int tsr_profile(tsr_ctx* c, int enable)
 {
     if (!c) return TSR_ERR_ARG;
     CK(cudaStreamSynchronize(c->stream));
+    if ((enable != 0) != c->prof) {
+        // the Arnoldi graphs carry timing events only while profiling
+        for (auto& g : c->graphs)
+            if (g) {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
+    }
     c->prof = enable != 0;
     c->prof_used = 0;
     for (int q = 0; q < 2; ++q) {
