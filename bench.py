@@ -796,7 +796,7 @@ def run_closure_bench(args):
         print(json.dumps({"metric": "learned-closure speed-up", "value": None, "error": fail_c}))
         return
     rc, wc, sc, fc, frac = res
-    resu, fail_u = attempt(params=closure.init_params(7), max_steps=600)
+    resu, fail_u = attempt(params=closure.init_params(7), max_steps=args.ablation_steps)
     ru, wu, su, fu, fracu = resu if resu is not None else ([], None, None, None, None)
 
     def errs(rec):
@@ -820,7 +820,8 @@ def run_closure_bench(args):
                     "errors": errs(rc), "out_of_range_at_t0": getattr(closure.run_closure, "ood_t0", None),
                     "flagged_per_step_first": flagged[:12], "flagged_total": int(sum(flagged))},
         "ablation_untrained": {"wall_s": wu, "steps": su, "fallback_fraction": fracu, "errors": errs(ru),
-                               "note": "untrained network (seed 7), at most 600 steps", "error": fail_u},
+                               "note": "untrained network (seed 7), at most %d steps" % args.ablation_steps,
+                               "error": fail_u},
         "training": {"samples": int(X.shape[0]), "data_s": t_data, "train_s": t_train,
                      "epochs": args.epochs, "loss": [float(x) for x in hist], "heldout": err,
                      "runs": desc},
@@ -858,6 +859,8 @@ def main():
     ap.add_argument("--closure-start", type=float, default=0.0,
                     help="config 5: plain method up to this time [d], then the closure")
     ap.add_argument("--epochs", type=int, default=8)
+    ap.add_argument("--ablation-steps", type=int, default=600,
+                    help="config 5: step cap of the untrained-network ablation run")
     ap.add_argument("--log-seconds", type=float, default=45.0)
     ap.add_argument("--scenarios", type=int, default=64)
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
