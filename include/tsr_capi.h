@@ -286,6 +286,13 @@ int tsr_closure_read(tsr_ctx* ctx, int* learned, double* kappa, int* flags);
  * flagged cells return to their micro meshes before the next step */
 int tsr_closure_attach(tsr_ctx* ctx, tsr_mlp* mlp, const double* norm, const float* zrange,
                        double thr, double qfloor, int auto_fallback);
+/* a second network of the same architecture and standardisation, trained
+ * from another seed (NULL detaches it): the coefficients become the mean of
+ * the two networks' outputs, and a cell is also flagged when the two
+ * networks' exchange inflows differ by more than thr_ens relative to
+ * max(inflow, qfloor) -- their disagreement stands for the error of the
+ * prediction, so a network that has not learned the closure is not used */
+int tsr_closure_attach_ensemble(tsr_ctx* ctx, tsr_mlp* second, double thr_ens);
 /* coefficients of the learned cells at the loaded state and the indicator */
 int tsr_closure_update(tsr_ctx* ctx, int* n_flagged);
 /* one accepted EXPREM step with the closure (update, fallback, step) */

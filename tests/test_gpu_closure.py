@@ -134,6 +134,61 @@ def test_closure_update_matches_oracle_network():
     net.close()
 
 
+def test_closure_ensemble_mean_and_disagreement_indicator():
+    """Two networks: the coefficients are the mean of the two outputs (two
+    copies of one network give that network's coefficients bit for bit and
+    flag nothing), and two different untrained networks disagree enough to
+    flag cells; against the oracle network, the mean of the two."""
+    p = P.config1()
+    p.set_learned(np.zeros(p.Ne, dtype=np.int32))
+    ctx = P.Context(p)
+    lib = ctx.lib
+    u = p.u0 + np.random.default_rng(5).uniform(-0.5, 0.5, p.N)
+    capi.check(lib.tsr_exprem_load(ctx.h, capi.ptr(u), 0.0), "load")
+    summ = np.empty(5 * p.Ne)
+    capi.check(lib.tsr_cell_summary(ctx.h, None, capi.ptr(summ)), "summary")
+    S = summ.reshape(p.Ne, 5)
+    capi.check(lib.tsr_closure_set_learned(ctx.h, np.ones(p.Ne, dtype=np.int32).ctypes.data_as(capi.ip)),
+               "relayout")
+    f = closure.features(S[:, 0], np.full((p.Ne, 3), np.nan), [0.0, -1e30, -1e30, -1e30], S[:, 1], S[:, 4])
+    fmu, fsd = f.mean(0), f.std(0) + 1e-3
+    norm = np.concatenate([fmu, fsd, [-8.0, -8.0], [1.5, 1.5]])
+    zr = np.concatenate([np.full(6, -1e3), np.full(6, 1e3)]).astype(np.float32)
+    pa, pb = om.init_params(21), om.init_params(22)
+    na, na2, nb = closure.Mlp(pa), closure.Mlp(pa), closure.Mlp(pb)
+    capi.check(lib.tsr_closure_attach(ctx.h, na.h, capi.ptr(norm), zr.ctypes.data_as(capi.fp), 1e-3, 0.0, 0),
+               "attach")
+    nf = C.c_int()
+    kap1, kap2, flags = np.empty(2 * p.Ne), np.empty(2 * p.Ne), np.empty(p.Ne, dtype=np.int32)
+    capi.check(lib.tsr_closure_update(ctx.h, C.byref(nf)), "update")
+    capi.check(lib.tsr_closure_read(ctx.h, None, capi.ptr(kap1), None), "read")
+    # the same network twice: the same coefficients, no disagreement
+    capi.check(lib.tsr_closure_attach_ensemble(ctx.h, na2.h, 1e-12), "ensemble")
+    capi.check(lib.tsr_closure_update(ctx.h, C.byref(nf)), "update")
+    capi.check(lib.tsr_closure_read(ctx.h, None, capi.ptr(kap2), flags.ctypes.data_as(capi.ip)), "read")
+    assert np.array_equal(kap1, kap2)
+    assert nf.value == 0 and not flags.any()
+    # two different networks: the mean of their outputs, and flags
+    capi.check(lib.tsr_closure_attach_ensemble(ctx.h, nb.h, 1e-2), "ensemble")
+    capi.check(lib.tsr_closure_update(ctx.h, C.byref(nf)), "update")
+    capi.check(lib.tsr_closure_read(ctx.h, None, capi.ptr(kap2), flags.ctypes.data_as(capi.ip)), "read")
+    assert nf.value == flags.sum() and nf.value > p.Ne // 2
+    x = np.zeros((p.Ne, 8), dtype=np.float32)
+    x[:, :6] = ((f - fmu) / fsd).astype(np.float32)
+    ya, _ = om.forward(pa, x, bf=True)
+    yb, _ = om.forward(pb, x, bf=True)
+    lq = 0.5 * ((ya[:, 0] * 1.5 - 8.0) + (yb[:, 0] * 1.5 - 8.0))
+    tol = 1.5 * 2e-3 * max(np.max(np.abs(ya)), np.max(np.abs(yb)))
+    assert np.max(np.abs(np.log(kap2[0::2]) - lq)) <= tol
+    # detached: back to the single network
+    capi.check(lib.tsr_closure_attach_ensemble(ctx.h, None, 0.0), "detach")
+    capi.check(lib.tsr_closure_update(ctx.h, C.byref(nf)), "update")
+    capi.check(lib.tsr_closure_read(ctx.h, None, capi.ptr(kap2), None), "read")
+    assert np.array_equal(kap1, kap2)
+    for n in (na, na2, nb):
+        n.close()
+
+
 def _mixed_problem():
     p = P.config1()
     rng = np.random.default_rng(3)

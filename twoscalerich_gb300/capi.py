@@ -180,6 +180,7 @@ _SIGNATURES = {
     "tsr_closure_set_coef": (C.c_int, [C.c_void_p, dp]),
     "tsr_closure_read": (C.c_int, [C.c_void_p, ip, dp, ip]),
     "tsr_closure_attach": (C.c_int, [C.c_void_p, C.c_void_p, dp, fp, C.c_double, C.c_double, C.c_int]),
+    "tsr_closure_attach_ensemble": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double]),
     "tsr_closure_update": (C.c_int, [C.c_void_p, ip]),
     "tsr_closure_advance": (C.c_int, [C.c_void_p, C.c_double, dp, dp, C.POINTER(ExpremOptions),
                                       C.POINTER(ExpremStats), dp, ip]),

@@ -143,8 +143,10 @@ def samples(p, logs, cell_stride=1, min_gap=1e-12, skip=0):
 class ClosureModel:
     """Network parameters and the standardisation of inputs and outputs."""
 
-    def __init__(self, params, fmu, fsd, ymu, ysd, zlo, zhi):
+    def __init__(self, params, fmu, fsd, ymu, ysd, zlo, zhi, params2=None):
         self.params = np.ascontiguousarray(params, dtype=np.float32)
+        # ensemble partner: the same network trained from another seed
+        self.params2 = None if params2 is None else np.ascontiguousarray(params2, dtype=np.float32)
         self.fmu, self.fsd = np.asarray(fmu, float), np.asarray(fsd, float)
         self.ymu, self.ysd = np.asarray(ymu, float), np.asarray(ysd, float)
         self.zlo, self.zhi = np.asarray(zlo, np.float32), np.asarray(zhi, np.float32)
@@ -156,13 +158,15 @@ class ClosureModel:
         return np.ascontiguousarray(np.concatenate([self.zlo, self.zhi]), dtype=np.float32)
 
     def save(self, path):
+        extra = {} if self.params2 is None else {"params2": self.params2}
         np.savez(path, params=self.params, fmu=self.fmu, fsd=self.fsd, ymu=self.ymu, ysd=self.ysd,
-                 zlo=self.zlo, zhi=self.zhi)
+                 zlo=self.zlo, zhi=self.zhi, **extra)
 
     @classmethod
     def load(cls, path):
         d = np.load(path)
-        return cls(d["params"], d["fmu"], d["fsd"], d["ymu"], d["ysd"], d["zlo"], d["zhi"])
+        return cls(d["params"], d["fmu"], d["fsd"], d["ymu"], d["ysd"], d["zlo"], d["zhi"],
+                   d["params2"] if "params2" in d.files else None)
 
 
 # parameter block of include/tsr_capi.h: (n_out, n_in) per layer, W then b
@@ -264,16 +268,24 @@ def standardise(X, Y, margin=0.25):
     return Xs, Ys, (fmu, fsd, ymu, ysd, zlo, zhi)
 
 
-def train_model(X, Y, epochs=8, batch=4096, lr=2e-3, wd=1e-4, seed=1001, holdout=0.05):
-    """Train the network on the GPU; returns (ClosureModel, epoch losses,
-    held-out relative errors of kQ and kT)."""
+def train_model(X, Y, epochs=8, batch=4096, lr=2e-3, wd=1e-4, seed=1001, holdout=0.05, ensemble=True):
+    """Train the network on the GPU (and, with ensemble, a second one from
+    seed + 1000 on the same standardised data: its disagreement with the
+    first is the closure's error indicator); returns (ClosureModel, epoch
+    losses of the first network, held-out relative errors of kQ and kT)."""
     rng = np.random.default_rng(seed)
     perm = rng.permutation(X.shape[0])
     nh = int(holdout * X.shape[0])
     Xs, Ys, st = standardise(X[perm[nh:]], Y[perm[nh:]])
     net = Mlp(init_params(seed))
     hist = net.train(Xs, Ys, epochs=epochs, batch=batch, lr=lr, wd=wd, seed=seed)
-    model = ClosureModel(net.get_params(), *st)
+    params2 = None
+    if ensemble:
+        net2 = Mlp(init_params(seed + 1000))
+        net2.train(Xs, Ys, epochs=epochs, batch=batch, lr=lr, wd=wd, seed=seed + 1000)
+        params2 = net2.get_params()
+        net2.close()
+    model = ClosureModel(net.get_params(), *st, params2=params2)
     err = None
     if nh > 0:
         err = heldout_error(net, model, X[perm[:nh]], Y[perm[:nh]])
@@ -320,16 +332,23 @@ def run_plain(p, times, max_steps=1000000):
 
 
 def run_closure(p, model, times, thr=1e-3, qfloor_rel=1e-3, auto_fallback=True, max_steps=1000000,
-                params=None, t_switch=0.0):
+                params=None, t_switch=0.0, thr_ens=None, params2=None):
     """The same run with the learned closure: the plain method up to
     t_switch (0: none), then every cell learned; flagged cells fall back to
-    their micro meshes.  Returns (records, wall seconds, steps, G
-    evaluations, fallback fraction per record time); the wall time includes
-    the plain start."""
+    their micro meshes.  thr_ens (with a second network, params2 or the
+    model's): the two-network ensemble and its disagreement indicator.
+    Returns (records, wall seconds, steps, G evaluations, fallback fraction
+    per record time); the wall time includes the plain start."""
     p.set_learned(np.zeros(p.Ne, dtype=np.int32))      # full layout, closure enabled
     ctx = P.Context(p)
     lib = ctx.lib
     net = Mlp(model.params if params is None else params)
+    net2 = None
+    if thr_ens is not None:
+        p2 = model.params2 if params2 is None else params2
+        if p2 is None:
+            raise ValueError("the ensemble indicator needs a second network")
+        net2 = Mlp(p2)
     check(lib.tsr_exprem_load(ctx.h, ptr(p.u0), 0.0), "load")
     st = capi.ExpremStats()
     t = C.c_double(0.0)
@@ -350,6 +369,8 @@ def run_closure(p, model, times, thr=1e-3, qfloor_rel=1e-3, auto_fallback=True, 
     norm, zr = model.norm(), model.zrange()      # alive for the duration of the calls
     check(lib.tsr_closure_attach(ctx.h, net.h, ptr(norm), zr.ctypes.data_as(capi.fp),
                                  thr, qfloor_rel * q0, int(auto_fallback)), "attach")
+    if net2 is not None:
+        check(lib.tsr_closure_attach_ensemble(ctx.h, net2.h, thr_ens), "attach ensemble")
     # inputs of the network at t = 0 against the accepted range (diagnostic)
     S0 = summ.reshape(-1, 5)
     f0 = features(S0[:, 0], np.full((p.Ne, 3), np.nan), [0.0, -1e30, -1e30, -1e30], S0[:, 1], S0[:, 4])
@@ -380,6 +401,8 @@ def run_closure(p, model, times, thr=1e-3, qfloor_rel=1e-3, auto_fallback=True, 
         w0 = time.perf_counter()
     ctx.close()
     net.close()
+    if net2 is not None:
+        net2.close()
     run_closure.ood_t0 = ood0
     run_closure.flagged_per_step = nfl
     return rec, wall, st.NumSteps, st.FuncEvals, frac

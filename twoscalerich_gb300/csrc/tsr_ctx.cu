@@ -153,6 +153,7 @@ struct tsr_ctx {
     int *d_hcount = nullptr, *d_flags = nullptr, *d_nflag = nullptr;
     double thist[3] = {0.0, 0.0, 0.0};
     tsr_mlp* mlp = nullptr;
+    tsr_mlp* mlp2 = nullptr;             // ensemble partner of mlp (or null)
     ClosureDev cdev{};
     bool auto_fallback = true;
     // set when a bounded wait of the closure network expired: its tensor
@@ -2216,6 +2217,8 @@ ClosureDev closure_dev(tsr_ctx* c)
     ClosureDev C = c->cdev;
     C.w = mlp_device_weights(c->mlp);
     C.p = mlp_device_params(c->mlp);
+    C.w2 = c->mlp2 ? mlp_device_weights(c->mlp2) : nullptr;
+    C.p2 = c->mlp2 ? mlp_device_params(c->mlp2) : nullptr;
     C.cells = c->d_lcells;
     C.n = c->nl;
     C.hist = c->d_hist;
@@ -2285,6 +2288,14 @@ extern "C" int tsr_closure_attach(tsr_ctx* c, tsr_mlp* mlp, const double* norm, 
     C.thr = thr;
     C.qfloor = qfloor;
     c->auto_fallback = auto_fallback != 0;
+    return TSR_OK;
+}
+
+extern "C" int tsr_closure_attach_ensemble(tsr_ctx* c, tsr_mlp* second, double thr_ens)
+{
+    if (!c || !c->closure || (second && !(thr_ens > 0.0))) return TSR_ERR_ARG;
+    c->mlp2 = second;
+    c->cdev.thr_ens = thr_ens;
     return TSR_OK;
 }
 

@@ -132,6 +132,9 @@ struct ClosureDev {
     int* nflag;                 // device counter
     double thr;                 // indicator threshold (relative flux change)
     double qfloor;              // flux floor of the relative measure
+    const void* w2;             // ensemble: the second network's bf16 weights (or null)
+    const float* p2;            // its FP32 parameter block
+    double thr_ens;             // threshold on the two networks' inflow difference
 };
 
 // Vector segments (one per scenario) for reductions and elementwise work.

@@ -1875,10 +1875,29 @@ __global__ void __launch_bounds__(128) k_closure_update(Problem P, const double*
     double Hc = 0.0, dth = 0.0;
     if (mine) closure_features(P, C, u, k, z, &ood, &Hc, &dth);
     auto x_at = [&](int, int c) -> float { return z[c]; };
-    auto out = [&](int, float o1, float o2) {
-        if (!mine) return;
-        const double y1 = (double)o1 * C.ysd[0] + C.ymu[0];
-        const double y2 = (double)o2 * C.ysd[1] + C.ymu[1];
+    // network A, then (ensemble) network B on the same tile and tensor memory
+    float oa[2] = {0.f, 0.f}, ob[2] = {0.f, 0.f};
+    uint32_t phase = 0;
+    auto out_a = [&](int, float o1, float o2) {
+        oa[0] = o1;
+        oa[1] = o2;
+    };
+    bool ok = tc_forward_tile(tcsm, tmem, C.p, x_at, out_a, phase, C.nflag + 1);
+    const bool two = C.w2 != nullptr;
+    if (two && ok) {
+        tc_stage_weights(reinterpret_cast<const __nv_bfloat16*>(C.w2), tcsm);
+        auto out_b = [&](int, float o1, float o2) {
+            ob[0] = o1;
+            ob[1] = o2;
+        };
+        ok = tc_forward_tile(tcsm, tmem, C.p2, x_at, out_b, phase, C.nflag + 1);
+    }
+    if (mine && ok) {
+        // the coefficients from the (mean) outputs
+        const double ya = (double)oa[0] * C.ysd[0] + C.ymu[0];
+        const double y1 = two ? 0.5 * (ya + ((double)ob[0] * C.ysd[0] + C.ymu[0])) : ya;
+        const double y2 = two ? 0.5 * (((double)oa[1] * C.ysd[1] + C.ymu[1]) + ((double)ob[1] * C.ysd[1] + C.ymu[1]))
+                              : (double)oa[1] * C.ysd[1] + C.ymu[1];
         const double sc = P.cell_scale ? P.cell_scale[k] : 1.0;
         const double kQ = exp(y1);
         const double kT = exp(y2) / ((sc * sc) * C.aint[P.m.cell_tpl_full[k]]);
@@ -1892,14 +1911,19 @@ __global__ void __launch_bounds__(128) k_closure_update(Problem P, const double*
             const double eta = fabs(kQ - kQold) * d / fmax(kQ * d, C.qfloor);
             if (eta > C.thr) flag = 1;
         }
+        // the two networks' inflows apart by more than thr_ens (relative to
+        // the inflow or the floor): the prediction is not to be trusted
+        if (two) {
+            const double qa = exp(ya), qb = exp((double)ob[0] * C.ysd[0] + C.ymu[0]);
+            const double eta = fabs(qa - qb) * d / fmax(kQ * d, C.qfloor);
+            if (eta > C.thr_ens) flag = 1;
+        }
         C.kappa[2 * k] = kQ;
         C.kappa[2 * k + 1] = kT;
         C.hcur[k] = Hc;
         C.flags[k] = flag;
         if (flag) atomicAdd(C.nflag, 1);
-    };
-    uint32_t phase = 0;
-    tc_forward_tile(tcsm, tmem, C.p, x_at, out, phase, C.nflag + 1);
+    }
     __syncthreads();
     tc_free(tmem);
 }
