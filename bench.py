@@ -772,7 +772,8 @@ def run_closure_bench(args):
         return
     t_all = time.perf_counter()
     msgs = []
-    X, Y, desc = closure.training_set(time_limit=args.log_seconds, log=lambda m: msgs.append(m))
+    X, Y, desc = closure.training_set(time_limit=args.log_seconds, log=lambda m: msgs.append(m),
+                                      t_stop=args.log_until)
     t_data = time.perf_counter() - t_all
     t0 = time.perf_counter()
     model, hist, err = closure.train_model(X, Y, epochs=args.epochs, batch=4096, lr=2e-3, seed=1001)
@@ -784,10 +785,12 @@ def run_closure_bench(args):
     # largest inflow of the field at t = 0 (norm-wise relative flux error)
     from twoscalerich_gb300.capi import TsrError
 
+    thr_ens = args.ens_indicator if args.ens_indicator > 0 else None
+
     def attempt(**kw):
         try:
             return closure.run_closure(mk(), model, times, thr=args.indicator, qfloor_rel=1.0,
-                                       t_switch=args.closure_start, **kw), None
+                                       t_switch=args.closure_start, thr_ens=thr_ens, **kw), None
         except TsrError as e:
             return None, str(e)
     res, fail_c = attempt()
@@ -796,7 +799,8 @@ def run_closure_bench(args):
         print(json.dumps({"metric": "learned-closure speed-up", "value": None, "error": fail_c}))
         return
     rc, wc, sc, fc, frac = res
-    resu, fail_u = attempt(params=closure.init_params(7), max_steps=args.ablation_steps)
+    resu, fail_u = attempt(params=closure.init_params(7), params2=closure.init_params(8),
+                           max_steps=args.ablation_steps)
     ru, wu, su, fu, fracu = resu if resu is not None else ([], None, None, None, None)
 
     def errs(rec):
@@ -810,17 +814,19 @@ def run_closure_bench(args):
         "ms_per_step": 1e3 * wc / max(sc, 1), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64 state, bf16 network", "data": "synthetic",
         "config": {"workload": "learned closure, two-scale Richards", "indicator_kind":
-                   "|dkQ| |theta_B(H_c) - theta| <= thr * max|Q(t=0)| per step, after 3 steps of history", "macro_nodes":
+                   "|dkQ| |theta_B(H_c) - theta| <= thr * max|Q(t=0)| per step, after 3 steps of history; "
+                   "two-network ensemble: |kQ_a - kQ_b| |theta_B(H_c) - theta| <= thr_ens * max(kQ |..|, max|Q(t=0)|)",
+                   "ensemble_indicator": thr_ens, "training_logs_until_d": args.log_until, "macro_nodes":
                    "%dx%d" % (args.n_macro, args.n_macro), "micro_nodes_per_cell":
                    "%dx%d" % (args.n_micro, args.n_micro), "cells": 2 * (args.n_macro - 1) ** 2,
                    "output_times_d": times, "indicator": args.indicator, "closure_start_d": args.closure_start,
-                   "network": "6 -> 4 x 64 SiLU -> 2, bf16 mma.sync, fp32 accumulation"},
+                   "network": "two networks 6 -> 4 x 64 SiLU -> 2 (seeds 1001, 2001), bf16 tcgen05 inference, fp32 accumulation"},
         "plain": {"wall_s": wp, "steps": sp, "g_evals": fp, "water": [r[1] for r in rp]},
         "closure": {"wall_s": wc, "steps": sc, "g_evals": fc, "fallback_fraction": frac,
                     "errors": errs(rc), "out_of_range_at_t0": getattr(closure.run_closure, "ood_t0", None),
                     "flagged_per_step_first": flagged[:12], "flagged_total": int(sum(flagged))},
         "ablation_untrained": {"wall_s": wu, "steps": su, "fallback_fraction": fracu, "errors": errs(ru),
-                               "note": "untrained network (seed 7), at most %d steps" % args.ablation_steps,
+                               "note": "untrained networks (seeds 7 and 8), at most %d steps" % args.ablation_steps,
                                "error": fail_u},
         "training": {"samples": int(X.shape[0]), "data_s": t_data, "train_s": t_train,
                      "epochs": args.epochs, "loss": [float(x) for x in hist], "heldout": err,
@@ -859,6 +865,10 @@ def main():
     ap.add_argument("--closure-start", type=float, default=0.0,
                     help="config 5: plain method up to this time [d], then the closure")
     ap.add_argument("--epochs", type=int, default=8)
+    ap.add_argument("--ens-indicator", type=float, default=0.05,
+                    help="config 5: threshold of the two-network disagreement indicator (0: one network)")
+    ap.add_argument("--log-until", type=float, default=None,
+                    help="config 5: training runs logged up to this time [d] (within --log-seconds)")
     ap.add_argument("--ablation-steps", type=int, default=600,
                     help="config 5: step cap of the untrained-network ablation run")
     ap.add_argument("--log-seconds", type=float, default=45.0)

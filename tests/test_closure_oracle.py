@@ -149,6 +149,9 @@ def test_samples_features_and_targets():
     X, Y = closure.samples(p, logs)
     assert X.shape[1] == 8 and Y.shape[1] == 2
     assert np.allclose(Y[:, 0], np.log(0.05), atol=1e-5)
+    # second target: log(Q / (s^2 A_int d theta/dt)) = log(0.1 / (s^2 A_int))
+    aint = closure.interior_area(p)
+    assert np.allclose(Y[:, 1].reshape(-1, p.Ne), np.log(0.1 / aint), atol=1e-5)
     # rate features: asinh(-0.1 / 0.1) = asinh(-1) once the history exists
     last = X[-p.Ne:]
     assert np.allclose(last[:, 1:4], np.arcsinh(-1.0), atol=1e-5)

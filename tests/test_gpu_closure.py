@@ -127,7 +127,7 @@ def test_closure_update_matches_oracle_network():
     x[:, :6] = ((f - fmu) / fsd).astype(np.float32)
     yo, _ = om.forward(params, x, bf=True)
     lq = yo[:, 0] * 1.5 - 8.0
-    lt = yo[:, 1] * 1.5 - 8.0 - np.log(closure.interior_area(p))
+    lt = lq - (yo[:, 1] * 1.5 - 8.0) - np.log(closure.interior_area(p))
     tol = 1.5 * 2e-3 * np.max(np.abs(yo))
     assert np.max(np.abs(np.log(kappa[0::2]) - lq)) <= tol
     assert np.max(np.abs(np.log(kappa[1::2]) - lt)) <= tol

@@ -13,10 +13,13 @@ smooth in every input and linear in theta.
 and the network predicts the coefficients from six inputs -- the macro
 head, its rates over the last three accepted steps, theta and h(theta):
 
-    kQ = exp(y1),   kT = exp(y2) / (s^2 A_int)
+    kQ = exp(y1),   kT = exp(y1 - y2) / (s^2 A_int)
 
 (s the cell's inclusion scale, A_int the template's interior CV area, so
-both outputs are free of the cell size).  The coefficients are evaluated
+both outputs are free of the cell size; y2 is the log of the ratio of the
+exchange inflow to the interior water rate s^2 A_int dtheta/dt, which the
+plain method keeps near a constant, so that the closure's water balance
+rests on one well-learned output instead of on two independent ones).  The coefficients are evaluated
 once per accepted step by the BF16 tensor-core network and held fixed
 during the step, so G stays smooth in FP64 and the finite-difference
 Jacobian of EXPREM sees the exact linearisation of the closure.
@@ -32,7 +35,7 @@ plain FP64 cell kernel for the rest of the run.
 Training data are logged from plain-method runs: after every accepted step
 the per-cell summary (tsr_cell_summary) gives H_c, theta, d theta/dt and Q
 of every cell, from which the inputs and the targets
-y1 = log(Q / d), y2 = log(s^2 A_int (d theta/dt) / d) are formed where both
+y1 = log(Q / d), y2 = log(Q / (s^2 A_int d theta/dt)) are formed where both
 ratios are positive.
 """
 import ctypes as C
@@ -87,9 +90,9 @@ def features(Hc, hist, t, th, hb):
     return f
 
 
-def log_plain_run(p, max_steps=100000, cell_stride=1, time_limit=None):
-    """Run the plain method on the GPU to p.tend and return, for every
-    accepted step, (t, summary[Ne, 5]) of every cell_stride-th cell."""
+def log_plain_run(p, max_steps=100000, cell_stride=1, time_limit=None, t_stop=None):
+    """Run the plain method on the GPU to p.tend (or t_stop) and return, for
+    every accepted step, (t, summary[Ne, 5]) of every cell_stride-th cell."""
     ctx = P.Context(p)
     lib = ctx.lib
     check(lib.tsr_exprem_load(ctx.h, ptr(p.u0), 0.0), "load")
@@ -101,8 +104,9 @@ def log_plain_run(p, max_steps=100000, cell_stride=1, time_limit=None):
     t0 = time.perf_counter()
     check(lib.tsr_cell_summary(ctx.h, None, ptr(out)), "summary")
     logs.append((0.0, out.reshape(p.Ne, 5)[::cell_stride].astype(np.float32)))
-    while t.value < p.tend and len(logs) <= max_steps:
-        check(lib.tsr_exprem_advance(ctx.h, p.tend, ptr(tspan), None, C.byref(p.options), C.byref(st),
+    t_end = p.tend if t_stop is None else min(p.tend, t_stop)
+    while t.value < t_end and len(logs) <= max_steps:
+        check(lib.tsr_exprem_advance(ctx.h, t_end, ptr(tspan), None, C.byref(p.options), C.byref(st),
                                      C.byref(t)), "advance")
         check(lib.tsr_cell_summary(ctx.h, None, ptr(out)), "summary")
         logs.append((t.value, out.reshape(p.Ne, 5)[::cell_stride].astype(np.float32)))
@@ -131,7 +135,10 @@ def samples(p, logs, cell_stride=1, min_gap=1e-12, skip=0):
         ok = np.abs(d) > min_gap
         ok[ok] = (Q[ok] / d[ok] > 0) & (rate[ok] / d[ok] > 0)
         y1 = np.log(Q[ok] / d[ok])
-        y2 = np.log(aint[ok] * rate[ok] / d[ok])
+        # second target: log of the exchange-to-interior-rate ratio
+        # Q / (s^2 A_int dtheta/dt), so that the closure's water balance
+        # depends on this (nearly constant) ratio alone
+        y2 = y1 - np.log(aint[ok] * rate[ok] / d[ok])
         X = np.zeros((ok.sum(), 8), dtype=np.float32)
         X[:, :N_FEAT] = f[ok]
         Xs.append(X)
@@ -298,7 +305,11 @@ def heldout_error(net, model, X, Y):
     Z = np.zeros_like(X)
     Z[:, :N_FEAT] = ((X[:, :N_FEAT] - model.fmu) / model.fsd).astype(np.float32)
     out = net.forward(Z).astype(np.float64) * model.ysd + model.ymu
-    rel = np.abs(np.expm1(out - Y.astype(np.float64)))
+    Yd = Y.astype(np.float64)
+    # log kQ = y1, log kT + log(s^2 A_int) = y1 - y2
+    lg = np.column_stack([out[:, 0], out[:, 0] - out[:, 1]])
+    lt = np.column_stack([Yd[:, 0], Yd[:, 0] - Yd[:, 1]])
+    rel = np.abs(np.expm1(lg - lt))
     return {"kQ_p50": float(np.median(rel[:, 0])), "kQ_p95": float(np.percentile(rel[:, 0], 95)),
             "kT_p50": float(np.median(rel[:, 1])), "kT_p95": float(np.percentile(rel[:, 1], 95))}
 
@@ -408,12 +419,12 @@ def run_closure(p, model, times, thr=1e-3, qfloor_rel=1e-3, auto_fallback=True, 
     return rec, wall, st.NumSteps, st.FuncEvals, frac
 
 
-def training_set(time_limit=45.0, skip=1, log=print):
+def training_set(time_limit=45.0, skip=1, log=print, t_stop=None, n_macro=101):
     """Training data from plain runs of the CPU-runnable configuration (two
     initial heads drawn from seeds 1001-1002) and of the GPU-scale plain
     configuration at 101 x 101 macro nodes (inclusion sizes and initial
-    noise from seeds 1001-1002), each run for at most time_limit seconds,
-    from step `skip` on (the early steps carry the fast decay of the initial
+    noise from seeds 1001-1002; n_macro), each run for at most time_limit
+    seconds and to at most t_stop days, from step `skip` on (the early steps carry the fast decay of the initial
     noise, whose head rates a closure run meets at its start too).  Returns
     (X, Y, description)."""
     X, Y, desc = [], [], []
@@ -428,12 +439,12 @@ def training_set(time_limit=45.0, skip=1, log=print):
         desc.append("21x21/11x11 h0=%.2f: %d steps to t=%.3g d, %d samples" % (h0, len(logs) - 1, logs[-1][0], len(x)))
         log(desc[-1])
     for seed in (1001, 1002):
-        q = P.config2(n_macro=101, seed=seed, eval_seed=seed + 1000)
-        logs = log_plain_run(q, cell_stride=2, time_limit=time_limit)
+        q = P.config2(n_macro=n_macro, seed=seed, eval_seed=seed + 1000)
+        logs = log_plain_run(q, cell_stride=2, time_limit=time_limit, t_stop=t_stop)
         x, y = samples(q, logs, cell_stride=2, skip=skip)
         X.append(x)
         Y.append(y)
-        desc.append("101x101/21x21 seed %d: %d steps to t=%.3g d, %d samples (every 2nd cell)"
-                    % (seed, len(logs) - 1, logs[-1][0], len(x)))
+        desc.append("%dx%d/21x21 seed %d: %d steps to t=%.3g d, %d samples (every 2nd cell)"
+                    % (n_macro, n_macro, seed, len(logs) - 1, logs[-1][0], len(x)))
         log(desc[-1])
     return np.concatenate(X), np.concatenate(Y), desc

@@ -1900,7 +1900,8 @@ __global__ void __launch_bounds__(128) k_closure_update(Problem P, const double*
                               : (double)oa[1] * C.ysd[1] + C.ymu[1];
         const double sc = P.cell_scale ? P.cell_scale[k] : 1.0;
         const double kQ = exp(y1);
-        const double kT = exp(y2) / ((sc * sc) * C.aint[P.m.cell_tpl_full[k]]);
+        // y2 = log of the exchange-to-interior-rate ratio
+        const double kT = exp(y1 - y2) / ((sc * sc) * C.aint[P.m.cell_tpl_full[k]]);
         const double d = fabs(dth);
         int flag = ood;
         const double kQold = C.kappa[2 * k];
