@@ -68,3 +68,25 @@ def test_checkpoint_resume_ensemble(tmp_path):
     ub = b.store()
     assert np.array_equal(ta, tb) and np.array_equal(ua, ub)
     assert all(sb[s].NumSteps == st[s].NumSteps and sb[s].FuncEvals == st[s].FuncEvals + 1 for s in range(3))
+
+
+def test_checkpoint_refused_by_closure_contexts(tmp_path):
+    """A learned-closure context neither writes nor reads checkpoints: its
+    head history, coefficients and cell layout are not in the file, so a
+    resumed run would not match its state (TSR_ERR_ARG both ways)."""
+    p = P.config1()
+    path = str(tmp_path / "plain.ckpt").encode()
+    a = P.Context(p)
+    lib = a.lib
+    capi.check(lib.tsr_exprem_load(a.h, capi.ptr(p.u0), 0.0), "load")
+    st = capi.ExpremStats()
+    _advance(lib, a.h, p, st, 3)
+    capi.check(lib.tsr_checkpoint_save(a.h, path, C.byref(st)), "save")
+    q = P.config1()
+    q.set_learned(np.zeros(q.Ne, dtype=np.int32))      # full layout, closure enabled
+    b = P.Context(q)
+    assert lib.tsr_num_unknowns(b.h) == p.N             # same unknown count as the file
+    capi.check(lib.tsr_exprem_load(b.h, capi.ptr(q.u0), 0.0), "load")
+    sb = capi.ExpremStats()
+    assert lib.tsr_checkpoint_load(b.h, path, C.byref(sb)) == 5
+    assert lib.tsr_checkpoint_save(b.h, str(tmp_path / "closure.ckpt").encode(), C.byref(sb)) == 5
