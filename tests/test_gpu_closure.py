@@ -137,8 +137,9 @@ def test_closure_update_matches_oracle_network():
 def test_closure_ensemble_mean_and_disagreement_indicator():
     """Two networks: the coefficients are the mean of the two outputs (two
     copies of one network give that network's coefficients bit for bit and
-    flag nothing), and two different untrained networks disagree enough to
-    flag cells; against the oracle network, the mean of the two."""
+    flag nothing), and a second network whose log-inflow output sits 0.1
+    higher (a shifted output bias) flags every cell with an inflow; against
+    the oracle network, the mean of the two."""
     p = P.config1()
     p.set_learned(np.zeros(p.Ne, dtype=np.int32))
     ctx = P.Context(p)
@@ -154,7 +155,10 @@ def test_closure_ensemble_mean_and_disagreement_indicator():
     fmu, fsd = f.mean(0), f.std(0) + 1e-3
     norm = np.concatenate([fmu, fsd, [-8.0, -8.0], [1.5, 1.5]])
     zr = np.concatenate([np.full(6, -1e3), np.full(6, 1e3)]).astype(np.float32)
-    pa, pb = om.init_params(21), om.init_params(22)
+    pa = om.init_params(21)
+    pb = pa.copy()
+    b5 = om.LAYOUT[-1][1]                  # bias of the output layer
+    pb[b5] += np.float32(0.1 / 1.5)        # log kQ + 0.1 (output std 1.5)
     na, na2, nb = closure.Mlp(pa), closure.Mlp(pa), closure.Mlp(pb)
     capi.check(lib.tsr_closure_attach(ctx.h, na.h, capi.ptr(norm), zr.ctypes.data_as(capi.fp), 1e-3, 0.0, 0),
                "attach")
@@ -169,10 +173,15 @@ def test_closure_ensemble_mean_and_disagreement_indicator():
     assert np.array_equal(kap1, kap2)
     assert nf.value == 0 and not flags.any()
     # two different networks: the mean of their outputs, and flags
-    capi.check(lib.tsr_closure_attach_ensemble(ctx.h, nb.h, 1e-2), "ensemble")
+    capi.check(lib.tsr_closure_attach_ensemble(ctx.h, nb.h, 0.05), "ensemble")
     capi.check(lib.tsr_closure_update(ctx.h, C.byref(nf)), "update")
     capi.check(lib.tsr_closure_read(ctx.h, None, capi.ptr(kap2), flags.ctypes.data_as(capi.ip)), "read")
-    assert nf.value == flags.sum() and nf.value > p.Ne // 2
+    d = np.abs(closure.theta_of(S[:, 0], P.SOIL_B) - S[:, 1])
+    assert nf.value == flags.sum() and nf.value >= np.count_nonzero(d > 0) - 2
+    # a looser threshold than the relative difference (e^0.1 - 1 = 0.105)
+    capi.check(lib.tsr_closure_attach_ensemble(ctx.h, nb.h, 0.2), "ensemble")
+    capi.check(lib.tsr_closure_update(ctx.h, C.byref(nf)), "update")
+    assert nf.value == 0
     x = np.zeros((p.Ne, 8), dtype=np.float32)
     x[:, :6] = ((f - fmu) / fsd).astype(np.float32)
     ya, _ = om.forward(pa, x, bf=True)
