@@ -93,7 +93,13 @@ def test_mlp_training_lowers_loss():
     hist = net.train(x, y, epochs=6, batch=1024, lr=3e-3, seed=1001)
     l1 = float(np.mean((net.forward(x) - y) ** 2))
     assert hist[-1] < hist[0] and l1 < 0.2 * l0, (hist, l0, l1)
+    # the gradient is summed over the batch's chunks in a fixed order, so a
+    # second training from the same seed gives the same parameters bit for bit
+    net2 = closure.Mlp(closure.init_params(1001))
+    net2.train(x, y, epochs=6, batch=1024, lr=3e-3, seed=1001)
+    assert np.array_equal(net.get_params(), net2.get_params())
     net.close()
+    net2.close()
 
 
 def test_closure_update_matches_oracle_network():
@@ -291,7 +297,7 @@ def test_closure_end_to_end_and_ablation():
     initial states from seeds 1001-1003), then (ablation) the held-out
     error of the closure coefficients with the trained network against the
     same network untrained, and the closure run (indicator 1e-3, fallback
-    on) against the plain run."""
+    on) against the plain run and against the untrained ablation."""
     X, Y = [], []
     for seed in (1001, 1002, 1003):
         q = P.config1()
@@ -313,12 +319,17 @@ def test_closure_end_to_end_and_ablation():
     trained.close()
     assert e_trained["kQ_p50"] < 0.5 * e_untrained["kQ_p50"], (e_trained, e_untrained)
     assert e_trained["kT_p50"] < 0.5 * e_untrained["kT_p50"], (e_trained, e_untrained)
-    # a short horizon: every fallback re-lays a cell out with a uniform
-    # interior, and the boundary layer that follows is a stiff transient the
-    # step control must resolve, so long closure runs take many steps
-    times = [0.005, 0.01]
+    # to 0.05 d: the trained closure keeps the total water within 1e-4 of
+    # the plain FP64 run at every output time, and closer to it than the
+    # same pipeline with untrained networks (whose near-zero outputs make a
+    # closure with the training data's mean coefficients)
+    times = [0.005, 0.01, 0.05]
     rec_p, wall_p, steps_p, evals_p = closure.run_plain(P.config1(), times)
     rec_c, wall_c, steps_c, evals_c, frac = closure.run_closure(P.config1(), model, times, qfloor_rel=1.0)
     ep = [abs(c[1] - r[1]) / r[1] for c, r in zip(rec_c, rec_p)]
-    assert max(ep) < 1e-2, ep
+    assert max(ep) <= 1e-4, ep
     assert all(0.0 <= f <= 1.0 for f in frac)
+    rec_u, _, _, _, _ = closure.run_closure(P.config1(), model, times, qfloor_rel=1.0,
+                                            params=closure.init_params(7))
+    eu = [abs(c[1] - r[1]) / r[1] for c, r in zip(rec_u, rec_p)]
+    assert all(a < b for a, b in zip(ep, eu)), (ep, eu)

@@ -5,8 +5,9 @@
 //   forward   Z_l = A_{l-1} W_l^T + b_l, A_l = SiLU(Z_l)   (one warp: 16 rows)
 //   loss      mean squared error over the 2 outputs
 //   backward  dZ_l = dA_l * SiLU'(Z_l), dA_{l-1} = dZ_l W_l (transposed
-//             weight copy), dW_l = dZ_l^T A_{l-1} (reduced over the batch
-//             in chunks of 256 rows, FP32 atomics), db_l = column sums
+//             weight copy), dW_l = dZ_l^T A_{l-1} and db_l = column sums,
+//             formed per chunk of 256 rows and summed over the chunks in
+//             ascending order (no atomics: training is reproducible)
 //   AdamW     on the FP32 master parameters, then the BF16 copies.
 // Every GEMM operand is rounded to BF16 where it is loaded, at the same
 // points as the fused inference kernel, so the training forward pass and
@@ -142,12 +143,16 @@ __global__ void k_layer_bwd_data(const float* __restrict__ dZ, int nout, int row
     }
 }
 
-// dW[nout x nin] += dZ^T X over a chunk of kChunk rows per block; one warp
-// per 16 output rows (m-tile), NT n-tiles over nin.  X row stride ldx.
+// The chunk's part of dW[nout x nin] = dZ^T X over kChunk rows per block,
+// written to dWp + blockIdx.x * kMlpParams (every element of the layer, one
+// thread each); k_chunk_sum then adds the chunks in ascending order, so the
+// gradient -- and training -- does not depend on the order blocks finish.
+// One warp per 16 output rows (m-tile), NT n-tiles over nin.  X row stride ldx.
 template <int NT>
 __global__ void k_layer_bwd_weight(const float* __restrict__ dZ, int nout, const float* __restrict__ X,
-                                   int ldx, int nin_valid, int rows, float* __restrict__ dW)
+                                   int ldx, int nin_valid, int rows, float* __restrict__ dWp)
 {
+    float* dW = dWp + (size_t)blockIdx.x * kMlpParams;
     const int mt = threadIdx.x >> 5;                 // m-tile of this warp
     if (16 * mt >= nout) return;
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
@@ -187,18 +192,19 @@ __global__ void k_layer_bwd_weight(const float* __restrict__ dZ, int nout, const
         const int c = 8 * n + 2 * t;
         const int oa = 16 * mt + g, ob = 16 * mt + g + 8;
         if (oa < nout) {
-            atomicAdd(dW + oa * nin + c, acc[n][0]);
-            atomicAdd(dW + oa * nin + c + 1, acc[n][1]);
+            dW[oa * nin + c] = acc[n][0];
+            dW[oa * nin + c + 1] = acc[n][1];
         }
         if (ob < nout) {
-            atomicAdd(dW + ob * nin + c, acc[n][2]);
-            atomicAdd(dW + ob * nin + c + 1, acc[n][3]);
+            dW[ob * nin + c] = acc[n][2];
+            dW[ob * nin + c + 1] = acc[n][3];
         }
     }
 }
 
-// db[o] += sum over a chunk of rows of dZ[row][o]
-__global__ void k_bias_grad(const float* __restrict__ dZ, int nout, int rows, float* __restrict__ db)
+// the chunk's part of db[o] = sum over its rows of dZ[row][o], at
+// dbp + blockIdx.x * kMlpParams
+__global__ void k_bias_grad(const float* __restrict__ dZ, int nout, int rows, float* __restrict__ dbp)
 {
     const int o = threadIdx.x;
     if (o >= nout) return;
@@ -206,7 +212,17 @@ __global__ void k_bias_grad(const float* __restrict__ dZ, int nout, int rows, fl
     const int i1 = min(rows, i0 + kChunk);
     float s = 0.0f;
     for (int i = i0; i < i1; ++i) s += dZ[(long long)i * nout + o];
-    atomicAdd(db + o, s);
+    dbp[(size_t)blockIdx.x * kMlpParams + o] = s;
+}
+
+// g[e] = sum over chunks c = 0, 1, ... of part[c][e] (fixed order)
+__global__ void k_chunk_sum(const float* __restrict__ part, int chunks, float* __restrict__ g)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= kMlpParams) return;
+    float s = 0.0f;
+    for (int c = 0; c < chunks; ++c) s += part[(size_t)c * kMlpParams + e];
+    g[e] = s;
 }
 
 // dZ = dA * SiLU'(Z), SiLU'(z) = s (1 + z (1 - s)), s = 1 / (1 + e^-z)
@@ -377,6 +393,7 @@ struct tsr_mlp {
     int cap = 0;
     float *b_x = nullptr, *b_y = nullptr, *d_loss = nullptr;
     float *z[5] = {}, *a[5] = {}, *dz = nullptr, *da = nullptr, *dx = nullptr;
+    float* gpart = nullptr;      // per-chunk gradient parts [chunks][kMlpParams]
     int step = 0;
     cudaStream_t s = nullptr;
     int* d_err = nullptr;
@@ -390,7 +407,7 @@ namespace {
 
 void mlp_free_batch(tsr_mlp* m)
 {
-    float** ps[] = {&m->b_x, &m->b_y, &m->d_loss, &m->dz, &m->da, &m->dx};
+    float** ps[] = {&m->b_x, &m->b_y, &m->d_loss, &m->dz, &m->da, &m->dx, &m->gpart};
     for (float** p : ps) {
         if (*p) cudaFree(*p);
         *p = nullptr;
@@ -414,6 +431,7 @@ int mlp_reserve(tsr_mlp* m, int rows)
     CKM(cudaMalloc(&m->dz, sizeof(float) * r * kMlpHidden));
     CKM(cudaMalloc(&m->da, sizeof(float) * r * kMlpHidden));
     CKM(cudaMalloc(&m->dx, sizeof(float) * r * kMlpHidden));
+    CKM(cudaMalloc(&m->gpart, sizeof(float) * ((r + kChunk - 1) / kChunk) * kMlpParams));
     for (int l = 0; l < 5; ++l) {
         const int w = (l == 4) ? kMlpOutPad : kMlpHidden;
         CKM(cudaMalloc(&m->z[l], sizeof(float) * r * w));
@@ -444,16 +462,16 @@ void forward_batch(tsr_mlp* m, int rows)
 // loss and gradients of a batch in b_x / b_y into d_g (zeroed first)
 int grad_batch(tsr_mlp* m, int rows)
 {
-    CKM(cudaMemsetAsync(m->d_g, 0, sizeof(float) * kMlpParams, m->s));
+    const int chunks = (rows + kChunk - 1) / kChunk;
+    CKM(cudaMemsetAsync(m->gpart, 0, sizeof(float) * (size_t)chunks * kMlpParams, m->s));
     CKM(cudaMemsetAsync(m->d_loss, 0, sizeof(float), m->s));
     forward_batch(m, rows);
     const int gb = warps_grid(rows);
-    const int chunks = (rows + kChunk - 1) / kChunk;
     k_loss<<<(rows + 255) / 256, 256, 0, m->s>>>(m->z[4], m->b_y, rows, m->dz, m->d_loss);
     // layer 5: dz holds dOut [rows x 8]
     k_layer_bwd_weight<8><<<chunks, 32, 0, m->s>>>(m->dz, kMlpOutPad, m->a[3], kMlpHidden, kMlpHidden, rows,
-                                                   m->d_g + kW5);
-    k_bias_grad<<<chunks, 64, 0, m->s>>>(m->dz, kMlpOutPad, rows, m->d_g + kB5);
+                                                   m->gpart + kW5);
+    k_bias_grad<<<chunks, 64, 0, m->s>>>(m->dz, kMlpOutPad, rows, m->gpart + kB5);
     k_layer_bwd_data<1, 8><<<gb, 128, 0, m->s>>>(m->dz, kMlpOutPad, rows, m->d_wt + kW5, m->da);
     const int wo[4] = {kW1, kW2, kW3, kW4};
     const int bo[4] = {kB1, kB2, kB3, kB4};
@@ -463,13 +481,14 @@ int grad_batch(tsr_mlp* m, int rows)
         const float* xin = (l == 0) ? m->b_x : m->a[l - 1];
         if (l == 0)
             k_layer_bwd_weight<2><<<chunks, 128, 0, m->s>>>(m->dz, kMlpHidden, xin, kRowStride, kMlpIn, rows,
-                                                            m->d_g + wo[l]);
+                                                            m->gpart + wo[l]);
         else
             k_layer_bwd_weight<8><<<chunks, 128, 0, m->s>>>(m->dz, kMlpHidden, xin, kMlpHidden, kMlpHidden, rows,
-                                                            m->d_g + wo[l]);
-        k_bias_grad<<<chunks, 64, 0, m->s>>>(m->dz, kMlpHidden, rows, m->d_g + bo[l]);
+                                                            m->gpart + wo[l]);
+        k_bias_grad<<<chunks, 64, 0, m->s>>>(m->dz, kMlpHidden, rows, m->gpart + bo[l]);
         if (l > 0) k_layer_bwd_data<4, 8><<<gb, 128, 0, m->s>>>(m->dz, kMlpHidden, rows, m->d_wt + wo[l], m->da);
     }
+    k_chunk_sum<<<(kMlpParams + 255) / 256, 256, 0, m->s>>>(m->gpart, chunks, m->d_g);
     CKM(cudaGetLastError());
     return TSR_OK;
 }
