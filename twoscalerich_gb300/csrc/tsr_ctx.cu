@@ -1652,7 +1652,7 @@ int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
         prof_end(c, pe);
         for (int q : pend) io.st[q].FuncEvals++;
         launch_err(c->d_g1, c->d_g0, V, N, c->d_coef + zoff, c->CS, c->d_mint + S, c->d_coef + doff, c->CS,
-                   c->d_winv, c->seg, scal_slot(c, S_ERR), HS, c->rw.partials, s);
+                   c->d_winv, c->seg, scal_slot(c, S_ERR), HS, c->rw.partials, c->d_w, s);
         CK(cudaGetLastError());
         if ((rc = read_flags(c))) return rc;
         if ((rc = fetch_scalars(c, S_ERR, errs.data()))) return rc;

@@ -231,9 +231,11 @@ void launch_winv(const double* u, double rtol, double atol, double* winv, const 
 void launch_combine(const double* u, const double* V, long long ldV, const double* c, int cstride,
                     const int* m, double* out, const SegInfo& g, cudaStream_t s);
 // res_s = sum ((g1 - g0 - sum_{q < mz_s} z_s[q] V_q) * dt3_s * winv)^2
+// the step error: D = (g1 - g0 - V z) dt/3 into D (a work vector), then
+// the weighted sum of squares of D into res
 void launch_err(const double* g1, const double* g0, const double* V, long long ldV, const double* z,
                 int zstride, const int* mz, const double* dt3, int dstride, const double* winv,
-                const SegInfo& g, double* res, int rstride, double* partials, cudaStream_t s);
+                const SegInfo& g, double* res, int rstride, double* partials, double* D, cudaStream_t s);
 
 // number of kernels this library has launched (host counter)
 unsigned long long kernel_launches();

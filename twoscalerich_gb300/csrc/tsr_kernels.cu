@@ -746,29 +746,6 @@ struct TermScaleWsq {
         return fma(r, r, a);
     }
 };
-struct TermErr {
-    const double* g1;
-    const double* g0;
-    const double* V;
-    long long ldV;
-    const double* z;
-    int zstride;
-    const int* mz;
-    const double* dt3;
-    int dstride;
-    const double* winv;
-    __device__ double operator()(int s, long long i, double a) const
-    {
-        const double* zs = z + (long long)s * zstride;
-        const int m = mz[s];
-        double d = g1[i] - g0[i];
-        for (int q = 0; q < m; ++q) d = fma(-zs[q], V[(long long)q * ldV + i], d);
-        double e = d * dt3[(long long)s * dstride];
-        double r = e * winv[i];
-        return fma(r, r, a);
-    }
-};
-
 template <class Term>
 static void run_reduce(const Term& t, const SegInfo& g, double* res, int rstride, double* partials,
                        cudaStream_t s)
@@ -817,13 +794,6 @@ void launch_scale_wsq(const double* w, const double* hsq, double* hn, double* ih
     count();
     k_store_sqrt<<<(g.nseg + 127) / 128, 128, 0, s>>>(hsq, hn, ih, stride, g.nseg, g.active);
     run_reduce(TermScaleWsq{w, ih, stride, v, winv}, g, res, stride, partials, s);
-}
-
-void launch_err(const double* g1, const double* g0, const double* V, long long ldV, const double* z,
-                int zstride, const int* mz, const double* dt3, int dstride, const double* winv,
-                const SegInfo& g, double* res, int rstride, double* partials, cudaStream_t s)
-{
-    run_reduce(TermErr{g1, g0, V, ldV, z, zstride, mz, dt3, dstride, winv}, g, res, rstride, partials, s);
 }
 
 // ---- fused Gram-Schmidt block of one Arnoldi step -----------------------------
@@ -1155,12 +1125,14 @@ int barrier_probe(int* timed_out)
     return 0;
 }
 
+static int g_nsm = 0;       // SMs of the device (set with the Gram-Schmidt launch shape)
 static constexpr int kGsMaxCluster = 16;
 static constexpr int kGsClusterSmem = kRedChunk * (int)sizeof(double);   // one chunk of a vector
 static int g_gs_cluster_max = 0;    // largest cluster the device schedules for the cluster kernel
 
 int gs_fused_grid(int nsm)
 {
+    g_nsm = nsm;
     int occ = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_gs_fused<false>, kRedThreads, 0) != cudaSuccess)
         return 0;
@@ -1540,6 +1512,37 @@ __global__ void __launch_bounds__(kRedThreads) k_segmap(Op op, SegInfo g)
     }
 }
 
+// The same elementwise work on a finer grid: block b covers part b % sub of
+// chunk b / sub (kRedChunk / sub items).  Elementwise results do not depend
+// on the mapping, so small problems (few chunks) spread over the whole GPU.
+template <class Op>
+__global__ void __launch_bounds__(kRedThreads) k_segmap_sub(Op op, SegInfo g, int sub)
+{
+    const SegBlock B = seg_block_at(g, (int)(blockIdx.x / (unsigned)sub));
+    if (g.active && !g.active[B.s]) return;
+    const int per = kRedChunk / sub;
+    const long long base =
+        B.lo + (long long)B.lb * kRedChunk + (long long)(blockIdx.x % (unsigned)sub) * per + threadIdx.x;
+    for (int q = 0; q < per / kRedThreads; ++q) {
+        const long long i = base + (long long)q * kRedThreads;
+        if (i < B.hi) op(B.s, i);
+    }
+}
+
+// chunk parts per block: the smallest power of two (at most 32) that gives
+// four blocks per SM, 1 for large problems
+template <class Op>
+static void segmap_launch(const Op& op, const SegInfo& g, cudaStream_t s)
+{
+    int sub = 1;
+    while (sub < kRedChunk / kRedThreads && (long long)g.nblocks * sub < 4LL * (g_nsm > 0 ? g_nsm : 152)) sub *= 2;
+    count();
+    if (sub == 1)
+        k_segmap<<<g.nblocks, kRedThreads, 0, s>>>(op, g);
+    else
+        k_segmap_sub<<<g.nblocks * sub, kRedThreads, 0, s>>>(op, g, sub);
+}
+
 struct OpScale {
     const double* x;
     const double* a;
@@ -1583,29 +1586,57 @@ struct OpCopy2 {
     }
 };
 
+// D = (g1 - g0 - sum_q z_q V_q) dt/3, the local error of the step
+struct OpErrD {
+    const double* g1;
+    const double* g0;
+    const double* V;
+    long long ldV;
+    const double* z;
+    int zstride;
+    const int* mz;
+    const double* dt3;
+    int dstride;
+    double* D;
+    __device__ void operator()(int s, long long i) const
+    {
+        const double* zs = z + (long long)s * zstride;
+        const int m = mz[s];
+        double d = g1[i] - g0[i];
+        for (int q = 0; q < m; ++q) d = fma(-zs[q], V[(long long)q * ldV + i], d);
+        D[i] = d * dt3[(long long)s * dstride];
+    }
+};
+
 void launch_seg_copy2(const double* a, double* b, const double* c, double* d, const SegInfo& g,
                       cudaStream_t s)
 {
-    count();
-    k_segmap<<<g.nblocks, kRedThreads, 0, s>>>(OpCopy2{a, b, c, d}, g);
+    segmap_launch(OpCopy2{a, b, c, d}, g, s);
 }
 void launch_seg_scale(const double* x, const double* a, int astride, double* y, const SegInfo& g,
                       cudaStream_t s)
 {
-    count();
-    k_segmap<<<g.nblocks, kRedThreads, 0, s>>>(OpScale{x, a, astride, y}, g);
+    segmap_launch(OpScale{x, a, astride, y}, g, s);
 }
 void launch_winv(const double* u, double rtol, double atol, double* winv, const SegInfo& g,
                  cudaStream_t s)
 {
-    count();
-    k_segmap<<<g.nblocks, kRedThreads, 0, s>>>(OpWinv{u, rtol, atol, winv}, g);
+    segmap_launch(OpWinv{u, rtol, atol, winv}, g, s);
 }
 void launch_combine(const double* u, const double* V, long long ldV, const double* c, int cstride,
                     const int* m, double* out, const SegInfo& g, cudaStream_t s)
 {
-    count();
-    k_segmap<<<g.nblocks, kRedThreads, 0, s>>>(OpCombine{u, V, ldV, c, cstride, m, out}, g);
+    segmap_launch(OpCombine{u, V, ldV, c, cstride, m, out}, g, s);
+}
+
+// the step's error in two passes, as the oracle forms it: D elementwise
+// (any grid), then the fixed-order weighted sum of squares of D
+void launch_err(const double* g1, const double* g0, const double* V, long long ldV, const double* z,
+                int zstride, const int* mz, const double* dt3, int dstride, const double* winv,
+                const SegInfo& g, double* res, int rstride, double* partials, double* D, cudaStream_t s)
+{
+    segmap_launch(OpErrD{g1, g0, V, ldV, z, zstride, mz, dt3, dstride, D}, g, s);
+    run_reduce(TermWsq{D, winv}, g, res, rstride, partials, s);
 }
 
 // ---- total water content --------------------------------------------------
