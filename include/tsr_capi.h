@@ -348,9 +348,11 @@ int tsr_set_calibrated_output(tsr_ctx* ctx, int enable);
  * (asynchronous on the context stream). */
 int tsr_calibrate_device(tsr_ctx* ctx, double* d_x);
 
-/* Gram-Schmidt block of an Arnoldi step as one cooperative launch (1, the
- * default) or as the j + 4 separate reduction launches (0).  Same results
- * either way. */
+/* Gram-Schmidt block of an Arnoldi step as one fused launch (1, the
+ * default), as the j + 4 separate reduction launches (0), or fused with
+ * problems of at most 16 chunks of 8,192 unknowns in one thread-block
+ * cluster (2) instead of spread one warp per CTA over the GPU (1).  Same
+ * results every way. */
 int tsr_set_fused_gs(tsr_ctx* ctx, int enable);
 
 /* Orthogonalisation of the Arnoldi step (the modified Gram-Schmidt loop

@@ -115,19 +115,21 @@ def test_dropin_gfunc_signature_path():
 
 
 def test_fused_gram_schmidt_matches_separate_kernels():
-    """the cooperative single-launch Gram-Schmidt block gives the same
-    trajectory, bit for bit, as the separate reduction launches"""
+    """the single-launch Gram-Schmidt block -- spread one warp per CTA over
+    the GPU (1) or in one thread-block cluster (2) -- gives the same
+    trajectory, bit for bit, as the separate reduction launches (0)"""
     p = P.config1()
     p.tend = 0.05
     p.tspan = np.array([1.0, 0.05])
     out = []
-    for fused in (1, 0):
+    for fused in (1, 2, 0):
         ctx = P.Context(p)
         capi.check(ctx.lib.tsr_set_fused_gs(ctx.h, fused), "tsr_set_fused_gs")
         out.append(P.run_to_end(ctx.exprem_step, p))
-    (ua, sa, sta, la), (ub, sb, stb, lb) = out
-    assert la == lb and np.array_equal(ua, ub) and np.array_equal(sa, sb)
-    assert sta.FuncEvals == stb.FuncEvals
+    (ua, sa, sta, la) = out[0]
+    for (ub, sb, stb, lb) in out[1:]:
+        assert la == lb and np.array_equal(ua, ub) and np.array_equal(sa, sb)
+        assert sta.FuncEvals == stb.FuncEvals
 
 
 @pytest.mark.parametrize("make", [lambda: P.config1(), lambda: P.fixture10()], ids=["config1", "fixture10_quads"])

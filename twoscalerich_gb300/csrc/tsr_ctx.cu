@@ -131,6 +131,10 @@ struct tsr_ctx {
     double* d_gs2part = nullptr;
     unsigned int* d_gsbar = nullptr;
     int* d_gserr = nullptr;
+    // problems of at most 16 chunks: Gram-Schmidt spread one warp per CTA
+    // over the GPU (1) or in one thread-block cluster (0); its warp sums
+    int gs_small_warps = 1;
+    double* d_gswpart = nullptr;
     std::vector<cudaGraphExec_t> graphs;
     std::vector<std::array<cudaEvent_t, 4>> graph_ev;
     double prof_acc_ms[2] = {0.0, 0.0}, prof_acc_bytes[2] = {0.0, 0.0};
@@ -802,6 +806,8 @@ int alloc_work(tsr_ctx* c, int max_krylov)
     CK(cudaMemset(c->d_gsbar, 0, sizeof(unsigned int) * 4));
     if ((rc = dev_alloc(c, sizeof(int) * 2, &p))) return rc;
     c->d_gserr = (int*)p;
+    if ((rc = dev_alloc(c, sizeof(double) * 256, &p))) return rc;
+    c->d_gswpart = (double*)p;
     CK(cudaMemset(c->d_gserr, 0, sizeof(int) * 2));
     c->gs_grid = gs_fused_grid(c->nsm);
     if (c->gs_grid < 1) c->fused_gs = false;
@@ -1295,7 +1301,9 @@ void arnoldi_kernels(tsr_ctx* c, int j, cudaEvent_t* ev, double frac)
         A.pstride = c->pstride;
         A.bar = c->d_gsbar;
         A.err = c->d_gserr;
-        if (!gs_fused_is_cluster(g, c->gs_grid)) cudaMemsetAsync(c->d_gsbar, 0, 2 * sizeof(unsigned int), s);
+        A.wpart = c->gs_small_warps ? c->d_gswpart : nullptr;
+        if (!gs_fused_is_cluster(g, c->gs_grid, A.wpart != nullptr))
+            cudaMemsetAsync(c->d_gsbar, 0, 2 * sizeof(unsigned int), s);
         launch_gs_fused(g, A, c->gs_grid, s);
     } else {
         launch_dot(c->d_w, V, g, Hc, HS, part, s);
@@ -2143,9 +2151,10 @@ extern "C" int tsr_set_gram_schmidt(tsr_ctx* c, int variant)
 
 extern "C" int tsr_set_fused_gs(tsr_ctx* c, int enable)
 {
-    if (!c) return TSR_ERR_ARG;
+    if (!c || enable < 0 || enable > 2) return TSR_ERR_ARG;
     CK(cudaStreamSynchronize(c->stream));
     c->fused_gs = enable != 0 && c->gs_grid > 0;
+    c->gs_small_warps = enable == 2 ? 0 : 1;
     for (auto& g : c->graphs)
         if (g) {
             cudaGraphExecDestroy(g);

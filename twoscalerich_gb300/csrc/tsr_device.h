@@ -205,6 +205,7 @@ struct GsArgs {
     long long parstride;        // CGS2: distance of the two partial buffers
     unsigned int* bar;          // [2] barrier count and generation
     int* err;                   // set if a barrier wait expired
+    double* wpart;              // 2 x 128 warp sums of the warp-spread kernel (or null)
 };
 int gs_fused_grid(int nsm);     // co-resident CTAs of the fused kernel
 // the grid barrier's bounded wait run out on purpose (a CTA that never
@@ -212,7 +213,9 @@ int gs_fused_grid(int nsm);     // co-resident CTAs of the fused kernel
 int barrier_probe(int* timed_out);
 cudaError_t launch_gs_fused(const SegInfo& g, const GsArgs& A, int max_grid, cudaStream_t s);
 // true if launch_gs_fused takes the cluster kernel (no grid barrier to reset)
-bool gs_fused_is_cluster(const SegInfo& g, int max_grid);
+// (warps: the caller passes the warp-sum buffer, so problems of at most 16
+// chunks take the warp-spread kernel; otherwise the one-cluster kernel)
+bool gs_fused_is_cluster(const SegInfo& g, int max_grid, bool warps);
 // classical Gram-Schmidt twice: co-resident CTAs for bases up to maxk + 1
 // vectors (0: cannot launch), the largest Krylov dimension it takes, launch
 int gs_cgs2_grid(int nsm, int maxk);

@@ -517,9 +517,9 @@ __global__ void __launch_bounds__(128) k_macro_nodes(Problem P, const double* __
                                                      const double* __restrict__ epsv,
                                                      double* __restrict__ out)
 {
-    __shared__ tsr_math_tables T;
-    load_tables(&T);
-    __syncthreads();
+    // one van Genuchten evaluation per thread: the math tables are read
+    // through L1 (staging all of them per CTA would cost more than the work)
+    const tsr_math_tables* T = &d_tables;
     const MacroDev& M = P.M;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= M.Mn) return;
@@ -540,7 +540,7 @@ __global__ void __launch_bounds__(128) k_macro_nodes(Problem P, const double* __
             acc = acc + tsr_u2d(tsr_d2u(c) ^ ((uint64_t)(ent & 1) << 63));
         }
         double Cn, Cd;
-        vg_storage(H, M.scen_pA ? M.scen_pA[sc] : P.pA, &T, Cn, Cd);
+        vg_storage(H, M.scen_pA ? M.scen_pA[sc] : P.pA, T, Cn, Cd);
         const double A = M.epsA * M.cv[i];
         const double den = fma(M.Ss, Cd, Cn) * A;
         g = (acc * Cd) / den;
@@ -1095,6 +1095,122 @@ __global__ void __launch_bounds__(kRedThreads, 1) k_gs_cluster(SegInfo g, GsArgs
     cl.sync();        // peers may still read this CTA's partials
 }
 
+// The Gram-Schmidt block for problems of at most 16 chunks, spread over the
+// GPU.  One pass of a chunk is 8,192 items x 2 FP64 fused multiply-adds;
+// with one CTA per chunk it runs on one SM, whose FP64 pipe issues one
+// warp instruction per 16 cycles (about 4 us a pass).  Here each of the
+// chunk's eight warps is a CTA of its own (up to 128 CTAs, one warp per
+// SM): thread l of CTA 8b + v plays thread 32v + l of chunk b in k_gs_fused
+// (same items, same chains), the warp's butterfly sum goes to global
+// memory, and after the bounded grid barrier every CTA forms the chunk
+// partials (the eight-warp tree of block_sum_256) and the segment total
+// (as segment_total forms it) itself -- the same bits.  w and the next
+// basis vector stay in registers, the current one in shared memory.
+__global__ void __launch_bounds__(32, 1) k_gs_warps(SegInfo g, GsArgs A)
+{
+    constexpr int Q = kRedChunk / kRedThreads;      // items per thread
+    __shared__ double vcs[Q * 32];                  // current basis vector, [q][lane]
+    const int j = A.j;
+    const int b = (int)(blockIdx.x >> 3), wv = (int)(blockIdx.x & 7);
+    const int lane = threadIdx.x;
+    const SegBlock B = seg_block_at(g, b);
+    const bool act = !(g.active && !g.active[B.s]);
+    const long long base = B.lo + (long long)B.lb * kRedChunk + wv * 32 + lane;
+    const long long so = (long long)B.s * A.stride;
+    const bool writer = (b == B.b0) && wv == 0 && lane == 0;
+    double w[Q], vn[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const long long i = base + (long long)q * kRedThreads;
+        const bool in = act && i < B.hi;
+        w[q] = in ? A.w[i] : 0.0;
+        vcs[q * 32 + lane] = in ? A.V[i] : 0.0;
+        vn[q] = (in && j >= 1) ? A.V[(size_t)A.ldV + i] : 0.0;
+    }
+    // total of the previous pass over this chunk's segment: chunk partials
+    // from their eight warp sums, then lane c holds 0 + P[c] and the block
+    // tree with the seven all-zero warps follows
+    auto seg_total = [&](int par) -> double {
+        const double* P = A.wpart + (size_t)par * 128;
+        double a = 0.0;
+        if (lane < B.nb) {
+            const double* c = P + (size_t)(B.b0 + lane) * 8;
+            const double cp = ((__ldcg(c) + __ldcg(c + 1)) + (__ldcg(c + 2) + __ldcg(c + 3))) +
+                              ((__ldcg(c + 4) + __ldcg(c + 5)) + (__ldcg(c + 6) + __ldcg(c + 7)));
+            a = 0.0 + cp;
+        }
+#pragma unroll
+        for (int d = 16; d >= 1; d >>= 1) a = a + __shfl_xor_sync(0xffffffffu, a, d);
+        const double z = 0.0;
+        return ((a + z) + (z + z)) + ((z + z) + (z + z));
+    };
+    for (int p = 0; p <= j + 2; ++p) {
+        double a = 0.0;
+        if (p == 0) {
+#pragma unroll
+            for (int q = 0; q < Q; ++q)
+                if (base + (long long)q * kRedThreads < B.hi) a = fma(w[q], vcs[q * 32 + lane], a);
+        } else {
+            const double h = seg_total((p + 1) & 1);
+            if (p <= j + 1) {
+                // h = H(p-1, j); w -= h v_{p-1}; dot with v_p (or with w after the last)
+                if (writer && act) A.Hc[so + p - 1] = h;
+#pragma unroll
+                for (int q = 0; q < Q; ++q) {
+                    if (base + (long long)q * kRedThreads >= B.hi) continue;
+                    const double wn = fma(-h, vcs[q * 32 + lane], w[q]);
+                    w[q] = wn;
+                    a = fma(wn, (p <= j) ? vn[q] : wn, a);
+                }
+            } else {
+                // h = ||w||^2: H(j+1, j) = sqrt, v_{j+1} = w / H(j+1, j), weighted norm
+                const double hn = sqrt(h);
+                const double ih = 1.0 / hn;
+                if (writer && act) {
+                    A.hsq[so] = h;
+                    A.Hc[so + j + 1] = hn;
+                    A.ih[so] = ih;
+                }
+                double* v = A.V + (size_t)(j + 1) * A.ldV;
+#pragma unroll
+                for (int q = 0; q < Q; ++q) {
+                    const long long i = base + (long long)q * kRedThreads;
+                    if (!act || i >= B.hi) continue;
+                    const double vv = w[q] * ih;
+                    v[i] = vv;
+                    const double rr = vv * vn[q];        // vn holds winv here
+                    a = fma(rr, rr, a);
+                }
+            }
+        }
+#pragma unroll
+        for (int d = 16; d >= 1; d >>= 1) a = a + __shfl_xor_sync(0xffffffffu, a, d);
+        if (lane == 0) A.wpart[(size_t)(p & 1) * 128 + (size_t)b * 8 + wv] = a;
+        if (p >= 1) {
+            // the next pass's vector: v_{p+1}, or the weights for the scaling pass
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                const long long i = base + (long long)q * kRedThreads;
+                const bool in = act && i < B.hi;
+                vcs[q * 32 + lane] = vn[q];
+                if (p + 1 <= j) vn[q] = in ? A.V[(size_t)(p + 1) * A.ldV + i] : 0.0;
+                else if (p + 1 == j + 2) vn[q] = in ? A.winv[i] : 0.0;
+            }
+        }
+        if (!grid_barrier(A.bar, A.bar + 1, gridDim.x, A.err)) return;
+    }
+    // the weighted norm of v_{j+1} (total of the last pass), then w
+    if (b == B.b0 && wv == 0 && act) {
+        const double sv = seg_total((j + 2) & 1);
+        if (lane == 0) A.sv[so] = sv;
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const long long i = base + (long long)q * kRedThreads;
+        if (act && i < B.hi) A.w[i] = w[q];
+    }
+}
+
 // Failure-path probe of the bounded grid barrier: CTA 1 leaves without
 // arriving, so CTA 0's wait must run out and raise *err.
 __global__ void k_barrier_probe(unsigned int* bar, int* err)
@@ -1166,10 +1282,18 @@ int gs_fused_grid(int nsm)
     return occ * nsm;
 }
 
-bool gs_fused_is_cluster(const SegInfo& g, int max_grid)
+// problems of at most 16 chunks take the warp-spread kernel when the caller
+// passes its warp-sum buffer (wpart), the one-cluster kernel otherwise
+static bool gs_use_warps(const SegInfo& g, int max_grid, bool warps)
 {
     const int grid = std::min(g.nblocks, max_grid);
-    return grid <= g_gs_cluster_max && grid == g.nblocks;
+    return warps && grid == g.nblocks && g.nblocks <= 16;
+}
+
+bool gs_fused_is_cluster(const SegInfo& g, int max_grid, bool warps)
+{
+    const int grid = std::min(g.nblocks, max_grid);
+    return !gs_use_warps(g, max_grid, warps) && grid <= g_gs_cluster_max && grid == g.nblocks;
 }
 
 cudaError_t launch_gs_fused(const SegInfo& g, const GsArgs& A, int max_grid, cudaStream_t s)
@@ -1184,6 +1308,14 @@ cudaError_t launch_gs_fused(const SegInfo& g, const GsArgs& A, int max_grid, cud
     cudaLaunchAttribute attr[1];
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    if (gs_use_warps(g, max_grid, A.wpart != nullptr)) {
+        // one 32-thread CTA per warp of every chunk, cooperative
+        cfg.gridDim = dim3((unsigned)(8 * g.nblocks));
+        cfg.blockDim = dim3(32);
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        return cudaLaunchKernelEx(&cfg, k_gs_warps, g, A);
+    }
     if (grid <= g_gs_cluster_max && grid == g.nblocks) {
         // one chunk per CTA, the whole grid one cluster
         attr[0].id = cudaLaunchAttributeClusterDimension;
