@@ -112,7 +112,7 @@ def test_cell_plans_give_identical_bits(make):
     ref = oracle.Oracle(p, nthreads=8).g(p.u0)
     plan = (C.c_int * 6)()
     for threads, budget, tables in ((224, 64 * 1024, 1), (224, 64 * 1024, 0), (448, 144 * 1024, 0),
-                                    (160, 48 * 1024, 1), (1024, 200 * 1024, 0)):
+                                    (160, 48 * 1024, 1), (1024, 200 * 1024, 0), (128, 0, 0), (128, 0, 1)):
         capi.check(lib.tsr_set_cell_plan(ctx.h, threads, budget, tables), "plan")
         capi.check(lib.tsr_cell_plan(ctx.h, plan), "read plan")
         assert plan[0] == threads and plan[2] == tables

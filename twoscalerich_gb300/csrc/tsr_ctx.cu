@@ -2016,7 +2016,10 @@ extern "C" int tsr_autotune(tsr_ctx* c, const double* u_host, int reps, double* 
     // counts of common templates evenly (the phases of a bundle wait for
     // their slowest warp)
     const int thr[] = {128, 160, 192, 224, 256, 288, 320, 384, 448, 512, 768, 1024};
-    const int bud[] = {48 * 1024, 64 * 1024, 96 * 1024, 144 * 1024, 200 * 1024};
+    // budgets from one cell per bundle (0: every CTA takes a single cell, the
+    // most CTAs for small problems, whose cells' long per-node chains then
+    // run side by side) to large bundles
+    const int bud[] = {0, 16 * 1024, 32 * 1024, 48 * 1024, 64 * 1024, 96 * 1024, 144 * 1024, 200 * 1024};
     double best = 1e30;
     int bt = c->tuned_threads, bb = c->tuned_budget;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
