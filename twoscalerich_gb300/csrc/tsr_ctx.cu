@@ -702,6 +702,8 @@ int build_problem(tsr_ctx* c, const user_data_struct& ud, const tsr_model_ext* e
     if ((rc = dev_alloc(c, sizeof(double) * 16 * (size_t)Ne, &p))) return rc;
     P.contrib = (double*)p;
     CK(cudaMemset(P.contrib, 0, sizeof(double) * 16 * (size_t)Ne));
+    if ((rc = dev_alloc(c, sizeof(double) * 2 * (size_t)(c->Mn > 0 ? c->Mn : 1), &p))) return rc;
+    P.node_st = (double*)p;
     if ((rc = dev_alloc(c, sizeof(int) * (size_t)(c->S + 3), &p))) return rc;
     P.flag = (int*)p;
     CK(cudaMemset(P.flag, 0, sizeof(int) * (size_t)(c->S + 3)));

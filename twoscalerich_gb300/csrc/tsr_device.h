@@ -104,6 +104,7 @@ struct Problem {
     int micro_grid;             // persistent grid of the cell kernel
     int misc_slots;             // per-cell scratch slots reserved in shared memory
     double* contrib;            // [16*Ne] macro contributions per element
+    double* node_st;            // [2*Mn] macro nodes' storage terms (Cd, den), from the cell kernel
     int* flag;                  // [nscen] device words: bit 0 non-finite G in scenario s
     const int* active;          // [nscen] scenarios to evaluate, or nullptr (all)
     int eps_stride;             // doubles between consecutive scenarios' {eps, 1/eps}

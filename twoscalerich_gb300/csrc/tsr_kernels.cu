@@ -292,7 +292,25 @@ __global__ void __launch_bounds__(1024) k_cells(Problem P, const double* __restr
     const MicroSet& S = P.m;
     const int nv = M.nv, Ne = M.Ne;
     const bool exch = (M.model_type == 3);
-    if (STAB) load_tables(reinterpret_cast<tsr_math_tables*>(sm));
+    if (STAB) {
+        load_tables(reinterpret_cast<tsr_math_tables*>(sm));
+        __syncthreads();
+    }
+    // The macro nodes' storage terms: their van Genuchten chains need only
+    // the state, so they run here, beside the cells, and k_macro_nodes
+    // keeps the gather and the division
+    for (int i = blockIdx.x * bs + tid; i < M.Mn; i += gridDim.x * bs) {
+        const int sc = M.nscen > 1 ? i / M.scen_nodes : 0;
+        if ((P.active && !P.active[sc]) || M.dirichlet[i]) continue;
+        const long long o = M.node_off ? M.node_off[i] : i;
+        const double eps = MODE ? epsv[(long long)sc * P.eps_stride] : 0.0;
+        const double H = state_at<MODE>(u, v, eps, o);
+        double Cn, Cd;
+        vg_storage(H, M.scen_pA ? M.scen_pA[sc] : P.pA, T, Cn, Cd);
+        const double A = M.epsA * M.cv[i];
+        P.node_st[2 * i] = Cd;
+        P.node_st[2 * i + 1] = fma(M.Ss, Cd, Cn) * A;
+    }
     int* cscen = ck + P.misc_slots;                          // scenario of each cell, -1 inactive
     for (int b = blockIdx.x; b < S.n_bundles; b += gridDim.x) {
         const int t = S.bundle_tpl[b], first = S.bundle_first[b], nc = S.bundle_count[b];
@@ -517,9 +535,7 @@ __global__ void __launch_bounds__(128) k_macro_nodes(Problem P, const double* __
                                                      const double* __restrict__ epsv,
                                                      double* __restrict__ out)
 {
-    // one van Genuchten evaluation per thread: the math tables are read
-    // through L1 (staging all of them per CTA would cost more than the work)
-    const tsr_math_tables* T = &d_tables;
+    // the storage terms (Cd, den) of every node come from the cell kernel
     const MacroDev& M = P.M;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= M.Mn) return;
@@ -530,8 +546,6 @@ __global__ void __launch_bounds__(128) k_macro_nodes(Problem P, const double* __
     if (M.dirichlet[i]) {
         g = 0.0;
     } else {
-        const double eps = MODE ? epsv[(long long)sc * P.eps_stride] : 0.0;
-        const double H = state_at<MODE>(u, v, eps, o);
         double acc = 0.0;
         const int p1 = M.csr_ptr[i + 1];
         for (int p = M.csr_ptr[i]; p < p1; ++p) {
@@ -539,10 +553,7 @@ __global__ void __launch_bounds__(128) k_macro_nodes(Problem P, const double* __
             const double c = P.contrib[ent >> 1];
             acc = acc + tsr_u2d(tsr_d2u(c) ^ ((uint64_t)(ent & 1) << 63));
         }
-        double Cn, Cd;
-        vg_storage(H, M.scen_pA ? M.scen_pA[sc] : P.pA, T, Cn, Cd);
-        const double A = M.epsA * M.cv[i];
-        const double den = fma(M.Ss, Cd, Cn) * A;
+        const double Cd = P.node_st[2 * i], den = P.node_st[2 * i + 1];
         g = (acc * Cd) / den;
     }
     if (!finite_d(g)) atomicOr(P.flag + sc, 1);
