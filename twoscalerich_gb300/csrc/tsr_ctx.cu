@@ -1285,7 +1285,6 @@ void arnoldi_kernels(tsr_ctx* c, int j, cudaEvent_t* ev, double frac)
         A.parstride = (long long)(c->maxk + 1) * c->pstride;
         A.bar = c->d_gsbar;
         A.err = c->d_gserr;
-        cudaMemsetAsync(c->d_gsbar, 0, 2 * sizeof(unsigned int), s);
         launch_gs_cgs2(g, A, c->gs2_grid, s);
     } else if (c->fused_gs) {
         GsArgs A{};
@@ -1304,8 +1303,9 @@ void arnoldi_kernels(tsr_ctx* c, int j, cudaEvent_t* ev, double frac)
         A.bar = c->d_gsbar;
         A.err = c->d_gserr;
         A.wpart = c->gs_small_warps ? c->d_gswpart : nullptr;
-        if (!gs_fused_is_cluster(g, c->gs_grid, A.wpart != nullptr))
-            cudaMemsetAsync(c->d_gsbar, 0, 2 * sizeof(unsigned int), s);
+        // the grid barrier's counters: every completed barrier leaves the
+        // count at 0 and only advances the generation, so they need no
+        // reset between launches (only after an expired wait, below)
         launch_gs_fused(g, A, c->gs_grid, s);
     } else {
         launch_dot(c->d_w, V, g, Hc, HS, part, s);
@@ -1520,6 +1520,7 @@ int exprem_round(tsr_ctx* c, const std::vector<int>& part, const RoundIO& io)
                 if (e) {
                     set_error("Gram-Schmidt: a grid barrier wait expired");
                     cudaMemset(c->d_gserr, 0, sizeof(int));
+                    cudaMemset(c->d_gsbar, 0, 2 * sizeof(unsigned int));   // a count left mid-barrier
                     return TSR_ERR_TIMEOUT;
                 }
             }

@@ -213,10 +213,6 @@ int gs_fused_grid(int nsm);     // co-resident CTAs of the fused kernel
 // arrives); *timed_out = 1 if the wait expired and raised its flag
 int barrier_probe(int* timed_out);
 cudaError_t launch_gs_fused(const SegInfo& g, const GsArgs& A, int max_grid, cudaStream_t s);
-// true if launch_gs_fused takes the cluster kernel (no grid barrier to reset)
-// (warps: the caller passes the warp-sum buffer, so problems of at most 16
-// chunks take the warp-spread kernel; otherwise the one-cluster kernel)
-bool gs_fused_is_cluster(const SegInfo& g, int max_grid, bool warps);
 // classical Gram-Schmidt twice: co-resident CTAs for bases up to maxk + 1
 // vectors (0: cannot launch), the largest Krylov dimension it takes, launch
 int gs_cgs2_grid(int nsm, int maxk);

@@ -1301,11 +1301,6 @@ static bool gs_use_warps(const SegInfo& g, int max_grid, bool warps)
     return warps && grid == g.nblocks && g.nblocks <= 16;
 }
 
-bool gs_fused_is_cluster(const SegInfo& g, int max_grid, bool warps)
-{
-    const int grid = std::min(g.nblocks, max_grid);
-    return !gs_use_warps(g, max_grid, warps) && grid <= g_gs_cluster_max && grid == g.nblocks;
-}
 
 cudaError_t launch_gs_fused(const SegInfo& g, const GsArgs& A, int max_grid, cudaStream_t s)
 {
