@@ -838,12 +838,12 @@ def run_closure_bench(args):
 # FP64 instructions (DADD + DMUL + DFMA, thread level) per unknown of one
 # finite-difference Jv launch of the cell kernel, and its DRAM bytes (read +
 # write) per unknown, from the ncu capture summarised in
-# profiles/k_cells_jv_141x141_21x21.md (version 8, captured on commit
-# a1d61c8, whose cell kernel is the current one: 1,027.3 M instructions and
-# 530.0 MB for 17,307,081 unknowns of the 141x141 / 21x21 case); both depend on the micro template (21x21 nodes), not on the macro
-# size, and are scaled by the unknowns.
-FP64_OPS_PER_UNKNOWN = {21: 59.36}
-G_TRAFFIC_PER_UNKNOWN = {21: 30.63}
+# profiles/k_cells_jv_141x141_21x21.md (version 9, the current cell kernel:
+# 1,027.5 M instructions and 530.3 MB for 17,307,081 unknowns of the
+# 141x141 / 21x21 case); both depend on the micro template (21x21 nodes),
+# not on the macro size, and are scaled by the unknowns.
+FP64_OPS_PER_UNKNOWN = {21: 59.37}
+G_TRAFFIC_PER_UNKNOWN = {21: 30.64}
 
 
 def main():
