@@ -849,7 +849,9 @@ __device__ __forceinline__ bool grid_barrier(unsigned int* count, unsigned int* 
         const unsigned int g0 = *vg;
         __threadfence();
         if (atomicAdd(count, 1u) == nblk - 1) {
-            atomicExch(count, 0u);
+            // every CTA has arrived, and none arrives at the next barrier
+            // before the generation moves: a plain store resets the count
+            *reinterpret_cast<volatile unsigned int*>(count) = 0u;
             __threadfence();
             atomicAdd(gen, 1u);
         } else {
@@ -1117,13 +1119,18 @@ __global__ void __launch_bounds__(kRedThreads, 1) k_gs_cluster(SegInfo g, GsArgs
 // partials (the eight-warp tree of block_sum_256) and the segment total
 // (as segment_total forms it) itself -- the same bits.  w and the next
 // basis vector stay in registers, the current one in shared memory.
-__global__ void __launch_bounds__(32, 1) k_gs_warps(SegInfo g, GsArgs A)
+template <int WPC>
+__global__ void __launch_bounds__(32 * WPC, 1) k_gs_warps(SegInfo g, GsArgs A)
 {
     constexpr int Q = kRedChunk / kRedThreads;      // items per thread
-    __shared__ double vcs[Q * 32];                  // current basis vector, [q][lane]
+    constexpr int NT = 32 * WPC;                    // threads per CTA
+    __shared__ double vcs[Q * NT];                  // current basis vector, [q][thread]
     const int j = A.j;
-    const int b = (int)(blockIdx.x >> 3), wv = (int)(blockIdx.x & 7);
-    const int lane = threadIdx.x;
+    const int cpb = 8 / WPC;                        // CTAs per chunk
+    const int b = (int)(blockIdx.x / (unsigned)cpb);
+    const int wv = (int)(blockIdx.x % (unsigned)cpb) * WPC + (int)(threadIdx.x >> 5);   // warp of the chunk
+    const int lane = threadIdx.x & 31;
+    const int tix = threadIdx.x;
     const SegBlock B = seg_block_at(g, b);
     const bool act = !(g.active && !g.active[B.s]);
     const long long base = B.lo + (long long)B.lb * kRedChunk + wv * 32 + lane;
@@ -1135,7 +1142,7 @@ __global__ void __launch_bounds__(32, 1) k_gs_warps(SegInfo g, GsArgs A)
         const long long i = base + (long long)q * kRedThreads;
         const bool in = act && i < B.hi;
         w[q] = in ? A.w[i] : 0.0;
-        vcs[q * 32 + lane] = in ? A.V[i] : 0.0;
+        vcs[q * NT + tix] = in ? A.V[i] : 0.0;
         vn[q] = (in && j >= 1) ? A.V[(size_t)A.ldV + i] : 0.0;
     }
     // total of the previous pass over this chunk's segment: chunk partials
@@ -1160,7 +1167,7 @@ __global__ void __launch_bounds__(32, 1) k_gs_warps(SegInfo g, GsArgs A)
         if (p == 0) {
 #pragma unroll
             for (int q = 0; q < Q; ++q)
-                if (base + (long long)q * kRedThreads < B.hi) a = fma(w[q], vcs[q * 32 + lane], a);
+                if (base + (long long)q * kRedThreads < B.hi) a = fma(w[q], vcs[q * NT + tix], a);
         } else {
             const double h = seg_total((p + 1) & 1);
             if (p <= j + 1) {
@@ -1169,7 +1176,7 @@ __global__ void __launch_bounds__(32, 1) k_gs_warps(SegInfo g, GsArgs A)
 #pragma unroll
                 for (int q = 0; q < Q; ++q) {
                     if (base + (long long)q * kRedThreads >= B.hi) continue;
-                    const double wn = fma(-h, vcs[q * 32 + lane], w[q]);
+                    const double wn = fma(-h, vcs[q * NT + tix], w[q]);
                     w[q] = wn;
                     a = fma(wn, (p <= j) ? vn[q] : wn, a);
                 }
@@ -1203,7 +1210,7 @@ __global__ void __launch_bounds__(32, 1) k_gs_warps(SegInfo g, GsArgs A)
             for (int q = 0; q < Q; ++q) {
                 const long long i = base + (long long)q * kRedThreads;
                 const bool in = act && i < B.hi;
-                vcs[q * 32 + lane] = vn[q];
+                vcs[q * NT + tix] = vn[q];
                 if (p + 1 <= j) vn[q] = in ? A.V[(size_t)(p + 1) * A.ldV + i] : 0.0;
                 else if (p + 1 == j + 2) vn[q] = in ? A.winv[i] : 0.0;
             }
@@ -1211,7 +1218,7 @@ __global__ void __launch_bounds__(32, 1) k_gs_warps(SegInfo g, GsArgs A)
         if (!grid_barrier(A.bar, A.bar + 1, gridDim.x, A.err)) return;
     }
     // the weighted norm of v_{j+1} (total of the last pass), then w
-    if (b == B.b0 && wv == 0 && act) {
+    if (b == B.b0 && wv == 0 && act) {             // warp 0 of the chunk, all its lanes
         const double sv = seg_total((j + 2) & 1);
         if (lane == 0) A.sv[so] = sv;
     }
@@ -1253,6 +1260,10 @@ int barrier_probe(int* timed_out)
 }
 
 static int g_nsm = 0;       // SMs of the device (set with the Gram-Schmidt launch shape)
+// warps of a chunk per CTA of the warp-spread Gram-Schmidt kernel (1, 2, 4
+// or 8): fewer CTAs make the grid barrier cheaper, more warps per SM make
+// the FP64 pipe the limit
+static constexpr int kGsWarpsPerCta = 1;
 static constexpr int kGsMaxCluster = 16;
 static constexpr int kGsClusterSmem = kRedChunk * (int)sizeof(double);   // one chunk of a vector
 static int g_gs_cluster_max = 0;    // largest cluster the device schedules for the cluster kernel
@@ -1315,12 +1326,12 @@ cudaError_t launch_gs_fused(const SegInfo& g, const GsArgs& A, int max_grid, cud
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     if (gs_use_warps(g, max_grid, A.wpart != nullptr)) {
-        // one 32-thread CTA per warp of every chunk, cooperative
-        cfg.gridDim = dim3((unsigned)(8 * g.nblocks));
-        cfg.blockDim = dim3(32);
+        // kGsWarpsPerCta warps of a chunk per CTA, cooperative
+        cfg.gridDim = dim3((unsigned)(8 / kGsWarpsPerCta * g.nblocks));
+        cfg.blockDim = dim3(32 * kGsWarpsPerCta);
         attr[0].id = cudaLaunchAttributeCooperative;
         attr[0].val.cooperative = 1;
-        return cudaLaunchKernelEx(&cfg, k_gs_warps, g, A);
+        return cudaLaunchKernelEx(&cfg, k_gs_warps<kGsWarpsPerCta>, g, A);
     }
     if (grid <= g_gs_cluster_max && grid == g.nblocks) {
         // one chunk per CTA, the whole grid one cluster
