@@ -58,6 +58,15 @@ int tsr_macro_mesh_build(int nv, int n_nodes, const double* xy, int n_elems,
                          const int* elems, int n_bedges, const int* bedges,
                          const int* macro_bc, macro_mesh_struct* mesh);
 
+/* The same arrays as tsr_macro_mesh_build (same arguments, same host
+ * struct, freed by tsr_macro_mesh_free) with the per-element geometry and
+ * the control-volume areas computed on the current GPU -- the step
+ * src/macro_mesh_properties.cpp:241-456 does on the host -- equal to the
+ * host builder's bit for bit. */
+int tsr_macro_mesh_build_device(int nv, int n_nodes, const double* xy, int n_elems,
+                                const int* elems, int n_bedges, const int* bedges,
+                                const int* macro_bc, macro_mesh_struct* mesh);
+
 /* Replaces micro_mesh_properties(const char*, micro_mesh_struct&)
  * (src/micro_mesh_properties.cpp:15; include/main.h:25). */
 int tsr_micro_mesh_properties(const char* mesh_file, micro_mesh_struct* mesh);

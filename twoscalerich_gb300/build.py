@@ -23,7 +23,7 @@ LIB = os.path.join(HERE, "libtsr_gb300.so")
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["tsr_kernels.cu", "tsr_ctx.cu", "tsr_noalloc.cu", "tsr_mlp.cu", "tsr_homog.cu"]
+CU_SOURCES = ["tsr_kernels.cu", "tsr_ctx.cu", "tsr_noalloc.cu", "tsr_mlp.cu", "tsr_homog.cu", "tsr_meshdev.cu"]
 CPP_SOURCES = ["tsr_host.cpp", "tsr_dropin.cpp"]
 
 

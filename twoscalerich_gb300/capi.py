@@ -103,6 +103,8 @@ _SIGNATURES = {
     "tsr_macro_mesh_properties": (C.c_int, [C.c_char_p, C.POINTER(MacroMesh), ip]),
     "tsr_macro_mesh_build": (C.c_int, [C.c_int, C.c_int, dp, C.c_int, ip, C.c_int, ip, ip,
                                        C.POINTER(MacroMesh)]),
+    "tsr_macro_mesh_build_device": (C.c_int, [C.c_int, C.c_int, dp, C.c_int, ip, C.c_int, ip, ip,
+                                       C.POINTER(MacroMesh)]),
     "tsr_micro_mesh_properties": (C.c_int, [C.c_char_p, C.POINTER(MicroMesh)]),
     "tsr_micro_mesh_build": (C.c_int, [C.c_double, C.c_double, C.c_int, C.c_int, dp, C.c_int,
                                        ip, C.c_int, ip, C.POINTER(MicroMesh)]),

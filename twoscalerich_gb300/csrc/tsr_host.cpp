@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "../../include/tsr_capi.h"
+#include "tsr_geom.h"
 #include "tsr_internal.h"
 
 namespace tsr {
@@ -47,116 +48,36 @@ static T* alloc_array(size_t n)
     return p;
 }
 
-static int orientation_sign(const double* xv, const double* yv, int nv)
+// Boundary condition types of the element edges (component-major, edge p
+// of element k at p*Ne+k) and which edges are on the boundary: tags -1..-5
+// mark nodes; an element edge whose two end nodes carry the same tag gets
+// that tag's BC type (later tags win), as the reference does
+// (src/macro_mesh_properties.cpp:76-104, 170-190).  Returns 1 if a
+// boundary edge names a node out of range.
+int macro_bc_edges(int nv, int Mn, int Ne, const int* elements, int n_bedges, const int* bedges,
+                   const int* macro_bc, int* bc_edges, unsigned char* is_bedge)
 {
-    // sum (x_{j+1} - x_j)(y_{j+1} + y_j) is positive for clockwise vertices
-    double s = 0.0;
-    for (int j = 0; j < nv; ++j) {
-        int jn = (j + 1) % nv;
-        s += (xv[jn] - xv[j]) * (yv[jn] + yv[j]);
-    }
-    return (s < 0.0) ? 1 : ((s > 0.0) ? -1 : 0);  // +1 for counter-clockwise
-}
-
-// Inverse of the n x n matrix M (row major) by Gauss-Jordan elimination with
-// partial pivoting; returns false if singular.
-static bool invert_small(int n, const double* M, double* Minv)
-{
-    double a[4][8];
-    for (int i = 0; i < n; ++i)
-        for (int j = 0; j < 2 * n; ++j)
-            a[i][j] = (j < n) ? M[i * n + j] : ((j - n == i) ? 1.0 : 0.0);
-    for (int c = 0; c < n; ++c) {
-        int p = c;
-        for (int r = c + 1; r < n; ++r)
-            if (std::fabs(a[r][c]) > std::fabs(a[p][c])) p = r;
-        if (a[p][c] == 0.0) return false;
-        if (p != c)
-            for (int j = 0; j < 2 * n; ++j) std::swap(a[p][j], a[c][j]);
-        double inv = 1.0 / a[c][c];
-        for (int j = 0; j < 2 * n; ++j) a[c][j] *= inv;
-        for (int r = 0; r < n; ++r) {
-            if (r == c || a[r][c] == 0.0) continue;
-            double f = a[r][c];
-            for (int j = 0; j < 2 * n; ++j) a[r][j] -= f * a[c][j];
+    std::vector<unsigned char> flag(5 * (size_t)Mn, 0);
+    for (int e = 0; e < n_bedges; ++e) {
+        int a = bedges[3 * e], b = bedges[3 * e + 1], tag = bedges[3 * e + 2];
+        if (a < 0 || a >= Mn || b < 0 || b >= Mn) return 1;
+        if (tag <= -1 && tag >= -5) {
+            int j = -tag - 1;
+            flag[(size_t)j * Mn + a] = 1;
+            flag[(size_t)j * Mn + b] = 1;
         }
     }
-    for (int i = 0; i < n; ++i)
-        for (int j = 0; j < n; ++j) Minv[i * n + j] = a[i][n + j];
-    return true;
-}
-
-// Element geometry shared by the macro and micro builders.
-struct ElemGeom {
-    int nv;
-    double cx, cy;
-    double scv[4];
-    double nrm[4][2];
-    double mid[4][2];        // SCV face midpoints
-    double sf[16];           // coefficient m of vertex i at m*nv+i
-    double blen[4][2];
-    double bmid[4][2][2];
-    double bnrm[4][2][2];
-};
-
-static bool element_geometry(int nv, const double* xv, const double* yv, ElemGeom& g)
-{
-    g.nv = nv;
-    g.cx = 0.0;
-    g.cy = 0.0;
-    for (int j = 0; j < nv; ++j) { g.cx += xv[j]; g.cy += yv[j]; }
-    g.cx /= (double)nv;
-    g.cy /= (double)nv;
-    int sgn = orientation_sign(xv, yv, nv);
-    double em[4][2];
-    for (int j = 0; j < nv; ++j) {
-        int jn = (j + 1) % nv;
-        em[j][0] = 0.5 * (xv[j] + xv[jn]);
-        em[j][1] = 0.5 * (yv[j] + yv[jn]);
-    }
-    for (int j = 0; j < nv; ++j) {
-        int jp = (j + nv - 1) % nv;
-        double d1x = g.cx - xv[j], d1y = g.cy - yv[j];
-        double d2x = em[j][0] - em[jp][0], d2y = em[j][1] - em[jp][1];
-        g.scv[j] = 0.5 * std::fabs(d1x * d2y - d1y * d2x);
-        double fx = g.cx - em[j][0], fy = g.cy - em[j][1];
-        g.nrm[j][0] = sgn * fy;
-        g.nrm[j][1] = -sgn * fx;
-        g.mid[j][0] = 0.5 * (em[j][0] + g.cx);
-        g.mid[j][1] = 0.5 * (em[j][1] + g.cy);
-        int jn = (j + 1) % nv;
-        double tx0 = em[j][0] - xv[j], ty0 = em[j][1] - yv[j];
-        double tx1 = xv[jn] - em[j][0], ty1 = yv[jn] - em[j][1];
-        g.blen[j][0] = std::sqrt(tx0 * tx0 + ty0 * ty0);
-        g.blen[j][1] = std::sqrt(tx1 * tx1 + ty1 * ty1);
-        g.bmid[j][0][0] = 0.5 * (xv[j] + em[j][0]);
-        g.bmid[j][0][1] = 0.5 * (yv[j] + em[j][1]);
-        g.bmid[j][1][0] = 0.5 * (xv[jn] + em[j][0]);
-        g.bmid[j][1][1] = 0.5 * (yv[jn] + em[j][1]);
-        g.bnrm[j][0][0] = sgn * ty0;
-        g.bnrm[j][0][1] = -sgn * tx0;
-        g.bnrm[j][1][0] = sgn * ty1;
-        g.bnrm[j][1][1] = -sgn * tx1;
-    }
-    // interpolant: rows of the vertex matrix are (x, y, 1) or (x, y, xy, 1);
-    // coefficient m of vertex i is Minv[m][i]
-    double M[16], Mi[16];
-    for (int i = 0; i < nv; ++i) {
-        if (nv == 3) {
-            M[i * 3 + 0] = xv[i];
-            M[i * 3 + 1] = yv[i];
-            M[i * 3 + 2] = 1.0;
-        } else {
-            M[i * 4 + 0] = xv[i];
-            M[i * 4 + 1] = yv[i];
-            M[i * 4 + 2] = xv[i] * yv[i];
-            M[i * 4 + 3] = 1.0;
-        }
-    }
-    if (!invert_small(nv, M, Mi)) return false;
-    for (int m = 0; m < nv; ++m)
-        for (int i = 0; i < nv; ++i) g.sf[m * nv + i] = Mi[m * nv + i];
-    return true;
+    for (int k = 0; k < Ne; ++k)
+        for (int j = 0; j < 5; ++j)
+            for (int p = 0; p < nv; ++p) {
+                int a = elements[(size_t)p * Ne + k];
+                int b = elements[(size_t)((p + 1) % nv) * Ne + k];
+                if (flag[(size_t)j * Mn + a] && flag[(size_t)j * Mn + b]) {
+                    bc_edges[(size_t)p * Ne + k] = macro_bc[j];
+                    is_bedge[(size_t)p * Ne + k] = 1;
+                }
+            }
+    return 0;
 }
 
 }  // namespace tsr
@@ -260,34 +181,13 @@ extern "C" int tsr_macro_mesh_build(int nv, int n_nodes, const double* xy, int n
     for (int k = 0; k < Ne; ++k)
         for (int v = 0; v < nv; ++v) m.elements[(size_t)v * Ne + k] = elems[(size_t)k * nv + v];
 
-    // boundary tags -1..-5 mark nodes; an element edge whose two end nodes
-    // carry the same tag gets that tag's BC type (later tags win), as the
-    // reference does (src/macro_mesh_properties.cpp:76-104, 170-190)
-    std::vector<unsigned char> flag(5 * (size_t)Mn, 0);
-    for (int e = 0; e < n_bedges; ++e) {
-        int a = bedges[3 * e], b = bedges[3 * e + 1], tag = bedges[3 * e + 2];
-        if (a < 0 || a >= Mn || b < 0 || b >= Mn) {
-            tsr_macro_mesh_free(out);
-            set_error("tsr_macro_mesh_build: boundary edge node out of range");
-            return TSR_ERR_BOUNDS;
-        }
-        if (tag <= -1 && tag >= -5) {
-            int j = -tag - 1;
-            flag[(size_t)j * Mn + a] = 1;
-            flag[(size_t)j * Mn + b] = 1;
-        }
-    }
     std::vector<unsigned char> is_bedge((size_t)nv * Ne, 0);
-    for (int k = 0; k < Ne; ++k)
-        for (int j = 0; j < 5; ++j)
-            for (int p = 0; p < nv; ++p) {
-                int a = m.elements[(size_t)p * Ne + k];
-                int b = m.elements[(size_t)((p + 1) % nv) * Ne + k];
-                if (flag[(size_t)j * Mn + a] && flag[(size_t)j * Mn + b]) {
-                    m.boundary_condition_edges[(size_t)p * Ne + k] = macro_bc[j];
-                    is_bedge[(size_t)p * Ne + k] = 1;
-                }
-            }
+    if (macro_bc_edges(nv, Mn, Ne, m.elements, n_bedges, bedges, macro_bc, m.boundary_condition_edges,
+                       is_bedge.data())) {
+        tsr_macro_mesh_free(out);
+        set_error("tsr_macro_mesh_build: boundary edge node out of range");
+        return TSR_ERR_BOUNDS;
+    }
 
     for (int k = 0; k < Ne; ++k) {
         double xv[4], yv[4];
