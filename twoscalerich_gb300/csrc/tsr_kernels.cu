@@ -1313,11 +1313,21 @@ static bool gs_use_warps(const SegInfo& g, int max_grid, bool warps)
 }
 
 
+// co-resident CTAs for nblocks chunks: as few rounds as max_grid allows, and
+// the chunks spread evenly over them (no half-empty last round); which CTA
+// forms a chunk's partial does not change it
+static int balanced_grid(int nblocks, int max_grid)
+{
+    if (nblocks <= max_grid || max_grid < 1) return std::min(nblocks, std::max(max_grid, 1));
+    const int rounds = (nblocks + max_grid - 1) / max_grid;
+    return (nblocks + rounds - 1) / rounds;
+}
+
 cudaError_t launch_gs_fused(const SegInfo& g, const GsArgs& A, int max_grid, cudaStream_t s)
 {
     count();
     cudaLaunchConfig_t cfg = {};
-    const int grid = std::min(g.nblocks, max_grid);
+    const int grid = balanced_grid(g.nblocks, max_grid);
     cfg.gridDim = dim3((unsigned)grid);
     cfg.blockDim = dim3(kRedThreads);
     cfg.dynamicSmemBytes = 0;
@@ -1627,7 +1637,7 @@ cudaError_t launch_gs_cgs2(const SegInfo& g, const GsArgs& A, int nsm, cudaStrea
     const int nv = A.j + 1;
     if (nv > kCgs2MaxNV || g_cgs2_occ[(nv - 1) / 8] < 1) return cudaErrorInvalidValue;
     cudaLaunchConfig_t cfg = {};
-    const int grid = std::min(g.nblocks, g_cgs2_occ[(nv - 1) / 8] * nsm);
+    const int grid = balanced_grid(g.nblocks, g_cgs2_occ[(nv - 1) / 8] * nsm);
     cfg.gridDim = dim3((unsigned)grid);
     cfg.blockDim = dim3(kRedThreads);
     cfg.dynamicSmemBytes = cgs2_smem(nv);
