@@ -79,3 +79,27 @@ def test_singular_denominator_returns_error_instead_of_exit():
     H = full_H(3, np.full((3, 4), np.nan))
     rc, _ = ours(3, 1.0, H)
     assert rc == 7          # TSR_ERR_SINGULAR; the reference calls exit() (src/phipade.cpp:160-166)
+
+
+def test_random_hessenberg_bitwise_against_oracle():
+    """The library's phi_1 (matrix products as interleaved FMA chains, work
+    matrices kept per thread) equals the oracle's plain loops bit for bit
+    on random upper Hessenberg matrices of every Krylov size up to 40 and
+    step sizes from 1e-4 to 1e3 (0 to about 20 squarings)."""
+    o = oracle.load()
+    rng = np.random.default_rng(17)
+    for m in range(1, MAXK + 1):
+        for alpha in (1e-4, 0.3, 7.0, 1e3):
+            Hc = np.zeros((m, m + 1))
+            for j in range(m):
+                Hc[j, :j + 2] = rng.normal(size=j + 2)
+                Hc[j, j + 1] = abs(Hc[j, j + 1]) + 0.1
+            H = full_H(m, Hc)
+            rc, phi = ours(m, alpha, H)
+            phio = np.zeros((MAXK, MAXK))
+            rco = o.oracle_phipade(capi.ptr(phio.ravel()), capi.ptr(H.ravel()), alpha, m, MAXK + 1, MAXK)
+            assert rc == rco
+            if rc == 0:
+                # the largest steps overflow where H has eigenvalues with a
+                # positive real part: the same NaNs on both sides
+                assert np.array_equal(phio, phi, equal_nan=True), (m, alpha)
